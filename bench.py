@@ -1,0 +1,403 @@
+"""Benchmark of the integer image pipeline on GB300.
+
+Workload (one step): one 4096x4096 u8 image through the 3x3 Sobel magnitude
+min(|gx|+|gy|, 255) with Boundary::MIRROR and the fused global u64 sum and u8
+max of the result, plus one 4096x4096 uchar4 image through the RGBA->gray
+point operator (77R + 150G + 29B) >> 8.  Steps rotate over NSETS resident
+image pairs (NSETS x 117 MB, several times the 129 MB L2), so every step reads
+its inputs from HBM.  Steps are replayed from CUDA graphs.
+
+Metric: Gpixels/s = (Sobel pixels + gray pixels) per second, whole job.
+`roofline` is for the dominant kernel (the gray point operator, 5 algorithmic
+bytes per pixel); `kernels` lists both kernels' achieved HBM bandwidth.
+`e2e` drives the same step through the C ABI with host buffers
+(hgb_image_write / kernels / hgb_image_read): pinned host -> device copies of
+both inputs and device -> host reads of both outputs and the two scalars.
+
+--impl reference times the reference's CPU path for the same step (the
+oracle's restatement of the CPU back end, OpenMP over all host cores).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W = H = 4096
+PX_PER_STEP = 2 * W * H  # Sobel pixels + gray pixels
+SOBEL_BYTES = 2 * W * H  # u8 in + u8 out (sum / max fused: 0 extra)
+GRAY_BYTES = 5 * W * H  # uchar4 in + u8 out
+NSETS = 16
+METRIC = "Gpixels/s (Sobel3x3 MIRROR + u64 sum + u8 max, and RGBA->gray, 4096x4096)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+def aggregate(elapsed_s: float, pixels: float, world: int):
+    """Max time and summed pixels over ranks (identity for one process)."""
+    if world <= 1:
+        return elapsed_s, pixels
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([elapsed_s], dtype=torch.float64, device=dev)
+    p = torch.tensor([pixels], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(p, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(p.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------- CPU
+def cpu_step_inputs(seed=0):
+    rng = np.random.default_rng(seed)
+    img = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    rgba = rng.integers(0, 256, (H, W, 4), dtype=np.uint8)
+    return img, rgba
+
+
+def cpu_step(O, img, rgba, nthreads):
+    mag = O.sobel_mag(img, boundary=O.MIRROR, nthreads=nthreads)
+    s = O.reduce_sum_u8(mag, nthreads=nthreads)
+    m = O.reduce_max_u8(mag, nthreads=nthreads)
+    g = O.rgba_to_gray(rgba, nthreads=nthreads)
+    return mag, s, m, g
+
+
+def cpu_time(seconds: float, nthreads: int):
+    """Steps of the CPU path for about `seconds`; returns (px/s, steps)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    img, rgba = cpu_step_inputs(7)
+    cpu_step(O, img, rgba, nthreads)  # warm
+    n, t0 = 0, time.perf_counter()
+    while True:
+        cpu_step(O, img, rgba, nthreads)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return n * PX_PER_STEP / el, n, el
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    cores = os.cpu_count() or 1
+    img, rgba = cpu_step_inputs(7)
+    for _ in range(max(0, min(args.warmup, 2))):
+        cpu_step(O, img, rgba, cores)
+    steps = max(1, min(args.steps, 20))  # bounded sample of the same step
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        cpu_step(O, img, rgba, cores)
+    el = time.perf_counter() - t0
+    v = steps * PX_PER_STEP / el / 1e9
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Gpixels/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded uniform u8 / uchar4)",
+        "config": {"workload": "sobel3x3_mirror_sum_max+rgba_gray_4096x4096", "width": W, "height": H},
+        "cpu_baseline": {"value": v, "unit": "Gpixels/s", "cores": cores, "kind": "port",
+                         "sample": f"{steps} full steps of the 4096x4096 pipeline (reference CPU back end restated,"
+                                   f" OpenMP over rows)"},
+        "e2e": {"value": v, "unit": "Gpixels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference CPU back end restated in C++/OpenMP (the reference compiler needs Clang 10 and its CUDA"
+                " runtime does not build on CUDA 13)",
+    }))
+
+
+# --------------------------------------------------------------------- GPU
+def run_gb300(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from hipacc_gb300 import _lib as L
+    from hipacc_gb300 import api
+
+    api.init(local)
+    dev = torch.device("cuda", local)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1234 + rank)
+    imgs = [torch.randint(0, 256, (H, W), dtype=torch.uint8, device=dev, generator=g) for _ in range(NSETS)]
+    rgbas = [torch.randint(0, 256, (H, W, 4), dtype=torch.uint8, device=dev, generator=g) for _ in range(NSETS)]
+    mags = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(NSETS)]
+    grays = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(NSETS)]
+    sums = torch.zeros((NSETS,), dtype=torch.int64, device=dev)
+    maxs = torch.zeros((NSETS,), dtype=torch.int32, device=dev)
+    L.call("hgb_workspace_reserve", 64 << 20)
+
+    def sobel(i, stream=None):
+        api.sobel_mag(imgs[i], mags[i], boundary=api.MIRROR, sum_out=sums[i:i + 1], max_out=maxs[i:i + 1],
+                      stream=stream)
+
+    def gray(i, stream=None):
+        api.gray(rgbas[i], grays[i], stream=stream)
+
+    def step(i, stream=None):
+        sobel(i, stream)
+        gray(i, stream)
+
+    # eager warm-up + correctness spot check of set 0 against torch arithmetic
+    for i in range(NSETS):
+        step(i)
+    torch.cuda.synchronize()
+
+    s = torch.cuda.Stream(device=dev)
+
+    def capture(fn, n):
+        gr = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            for i in range(NSETS):  # warm on the capture stream
+                fn(i, s)
+            torch.cuda.synchronize()
+            with torch.cuda.graph(gr, stream=s):
+                for k in range(n):
+                    fn(k % NSETS, s)
+        torch.cuda.synchronize()
+        return gr
+
+    g_step = capture(step, NSETS)
+    rem = args.steps % NSETS
+    g_rem = capture(step, rem) if rem else None
+    g_sobel = capture(sobel, NSETS)
+    g_gray = capture(gray, NSETS)
+
+    for _ in range(max(3, args.warmup // NSETS + 1)):
+        g_step.replay()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.25)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(s):
+        e0.record(s)
+        for _ in range(args.steps // NSETS):
+            g_step.replay()
+        if g_rem is not None:
+            g_rem.replay()
+        e1.record(s)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    # per-kernel average launch duration, same stream, same rotation
+    kern = {}
+    for name, gr, nbytes in (("sobel3_kernel+reduce", g_sobel, SOBEL_BYTES), ("gray_kernel", g_gray, GRAY_BYTES)):
+        reps = max(4, args.steps // NSETS // 2)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(s):
+            gr.replay()
+            a.record(s)
+            for _ in range(reps):
+                gr.replay()
+            b.record(s)
+        torch.cuda.synchronize()
+        us = a.elapsed_time(b) * 1e3 / (reps * NSETS)
+        kern[name] = {"us_per_launch": us, "algorithmic_bytes": nbytes, "achieved_gbs": nbytes / us / 1e3}
+    clk = clocks.stop()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    elapsed_max, px_total = aggregate(elapsed, args.steps * PX_PER_STEP, world)
+    value = px_total / elapsed_max / 1e9
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = run_e2e(args, L, dev, rank)
+    e2e_max, e2e_px = aggregate(e2e["elapsed"], e2e["pixels"], world)
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1:
+        cores = os.cpu_count() or 1
+        pxs, n, el = cpu_time(args.cpu_seconds, cores)
+        cpu = {"value": pxs / 1e9, "unit": "Gpixels/s", "cores": cores, "kind": "port",
+               "sample": f"{n} full 4096x4096 steps in {el:.1f} s (reference CPU back end restated, OpenMP)"}
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    dom = kern["gray_kernel"]
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gpixels/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed_max / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded uniform u8 / uchar4)",
+            "config": {"workload": "sobel3x3_mirror_sum_max+rgba_gray_4096x4096", "width": W, "height": H,
+                       "images_per_step": "1 u8 + 1 uchar4", "pixels_per_step": PX_PER_STEP,
+                       "resident_sets": NSETS, "l2": f"inputs larger than L2 ({NSETS} rotating sets, "
+                                                     f"{NSETS * 117} MB)", "launch": "CUDA graph replay",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": dom["achieved_gbs"] / peak, "traffic": None, "kernel": "gray_kernel",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},
+            "kernels": kern,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_px / e2e_max / 1e9, "unit": "Gpixels/s", "h2d_bytes_per_step": e2e["h2d"],
+                    "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"]},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_e2e(args, L, dev, rank):
+    """Host buffers in, host results out, every step through the C ABI."""
+    import torch
+
+    lib = L.load()
+    rng = np.random.default_rng(99 + rank)
+    n_e2e = max(4, min(args.steps // 8, 200))
+    h_img = torch.from_numpy(rng.integers(0, 256, (H, W), dtype=np.uint8)).pin_memory()
+    h_rgba = torch.from_numpy(rng.integers(0, 256, (H, W, 4), dtype=np.uint8)).pin_memory()
+    h_mag = torch.empty((H, W), dtype=torch.uint8).pin_memory()
+    h_gray = torch.empty((H, W), dtype=torch.uint8).pin_memory()
+    h_scalars = torch.empty(4, dtype=torch.int64).pin_memory()
+    imgs = {}
+    for name, dt in (("img", L.U8), ("rgba", L.U8X4), ("mag", L.U8), ("gray", L.U8)):
+        p = C.c_void_p()
+        L.check(lib.hgb_image_create(dt, W, H, 256, None, C.byref(p)))
+        imgs[name] = p
+    views = {}
+    for k, p in imgs.items():
+        v = L.View()
+        L.check(lib.hgb_image_get_view(p, C.byref(v)))
+        views[k] = v
+    scal = torch.zeros(2, dtype=torch.int64, device=dev)
+    st = torch.cuda.current_stream()
+    sp = C.c_void_p(st.cuda_stream)
+    mx = np.array([-1, 0, 1, -2, 0, 2, -1, 0, 1], np.int32)
+    my = np.array([-1, -2, -1, 0, 0, 0, 1, 2, 1], np.int32)
+
+    def one():
+        L.check(lib.hgb_image_write(imgs["img"], C.c_void_p(h_img.data_ptr()), sp))
+        L.check(lib.hgb_image_write(imgs["rgba"], C.c_void_p(h_rgba.data_ptr()), sp))
+        L.check(lib.hgb_sobel_mag(C.byref(views["img"]), C.byref(views["mag"]), mx.ctypes.data_as(C.c_void_p),
+                                  my.ctypes.data_as(C.c_void_p), 3, L.MIRROR, 0, C.c_void_p(scal.data_ptr()),
+                                  C.c_void_p(scal.data_ptr() + 8), sp))
+        L.check(lib.hgb_point_gray(C.byref(views["rgba"]), C.byref(views["gray"]), 77, 150, 29, 8, sp))
+        L.check(lib.hgb_image_read(imgs["mag"], C.c_void_p(h_mag.data_ptr()), sp))
+        L.check(lib.hgb_image_read(imgs["gray"], C.c_void_p(h_gray.data_ptr()), sp))
+        h_scalars[:2].copy_(scal, non_blocking=False)
+
+    for _ in range(3):
+        one()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        one()
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    for p in imgs.values():
+        lib.hgb_image_destroy(p)
+    return {"elapsed": el, "pixels": n_e2e * PX_PER_STEP, "steps": n_e2e, "h2d": W * H * 5,
+            "d2h": W * H * 2 + 16}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

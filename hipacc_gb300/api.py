@@ -1,0 +1,191 @@
+"""Python front end of the C ABI for torch CUDA tensors.
+
+Images are tensors of shape (H, W) or (B, H, W); RGBA images are uint8
+tensors of shape (H, W, 4) or (B, H, W, 4).  Every call goes through
+libhipacc_gb300.so on the tensor's device and current stream; nothing here
+computes pixels itself.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import struct
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from ._lib import CLAMP, CONSTANT, MAX, MIN, MIRROR, PROD, REPEAT, SUM, UNDEFINED  # noqa: F401
+
+_DT = {torch.uint8: L.U8, torch.int16: L.I16, torch.int32: L.I32, torch.float16: L.F16,
+       torch.bfloat16: L.BF16, torch.float32: L.F32, torch.float64: L.F64, torch.int64: L.U64}
+
+SOBEL3_X = np.array([[-1, 0, 1], [-2, 0, 2], [-1, 0, 1]], np.int32)
+SOBEL3_Y = np.array([[-1, -2, -1], [0, 0, 0], [1, 2, 1]], np.int32)
+
+
+def view(t: torch.Tensor, rgba: bool = False) -> L.View:
+    """hgb_view of a CUDA tensor (rows may be padded; the last dim must be dense)."""
+    if not t.is_cuda:
+        raise ValueError("hipacc_gb300 operates on CUDA tensors")
+    es = t.element_size()
+    if rgba:
+        if t.dtype != torch.uint8 or t.shape[-1] != 4 or t.stride(-1) != 1 or t.stride(-2) != 4:
+            raise ValueError("RGBA images are uint8 tensors (..., H, W, 4) with dense pixels")
+        shape = t.shape[:-1]
+        strides = t.stride()[:-1]
+        dt = L.U8X4
+    else:
+        if t.stride(-1) != 1:
+            raise ValueError("the innermost dimension must be dense")
+        shape, strides, dt = t.shape, t.stride(), _DT[t.dtype]
+    if len(shape) == 2:
+        b, (h, w) = 1, shape
+        bs = strides[0] * es * h
+    elif len(shape) == 3:
+        b, h, w = shape
+        bs = strides[0] * es
+    else:
+        raise ValueError("images are (H, W) or (B, H, W)")
+    pitch = strides[-2] * es
+    return L.View(t.data_ptr(), dt, int(w), int(h), int(b), int(pitch), int(bs))
+
+
+def window(w):
+    if w is None:
+        return None
+    return C.byref(L.Window(*[int(v) for v in w]))
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _fptr(a):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, np.float32)
+    return a.ctypes.data_as(C.c_void_p), a
+
+
+def init(device: int = 0) -> str:
+    buf = C.create_string_buffer(256)
+    L.call("hgb_init", device, buf, 256)
+    return buf.value.decode()
+
+
+def local_op(inp, out=None, mask=None, domain=None, size=None, reduce=SUM, boundary=CLAMP, const=0.0, acc=None,
+             iter_space=None, mask_dev=None, stream=None):
+    """Kernel::convolve / reduce(Domain) as one launch (hgb_local_op)."""
+    if out is None:
+        out = torch.empty_like(inp)
+    if mask is not None:
+        m = np.ascontiguousarray(mask, np.float32)
+        mh, mw = m.shape
+    elif mask_dev is not None:
+        mh, mw = size
+        m = None
+    else:
+        mh, mw = size if size is not None else np.asarray(domain).shape
+        m = None
+    d = None if domain is None else np.ascontiguousarray(domain, np.uint8)
+    vi, vo = view(inp), view(out)
+    L.call("hgb_local_op", C.byref(vi), window(acc), C.byref(vo), window(iter_space),
+           None if m is None else m.ctypes.data_as(C.c_void_p),
+           None if mask_dev is None else C.c_void_p(mask_dev.data_ptr()),
+           None if d is None else d.ctypes.data_as(C.c_void_p), mw, mh, reduce, boundary, float(const),
+           _stream(stream))
+    return out
+
+
+def sobel_mag(inp, out=None, mask_x=SOBEL3_X, mask_y=SOBEL3_Y, boundary=MIRROR, const=0, sum_out=None, max_out=None,
+              stream=None):
+    """Sobel magnitude with fused u64 sum / u8 max (device tensors of 1 int64 / int32)."""
+    if out is None:
+        out = torch.empty_like(inp)
+    mx = np.ascontiguousarray(mask_x, np.int32)
+    my = np.ascontiguousarray(mask_y, np.int32)
+    vi, vo = view(inp), view(out)
+    L.call("hgb_sobel_mag", C.byref(vi), C.byref(vo), mx.ctypes.data_as(C.c_void_p), my.ctypes.data_as(C.c_void_p),
+           mx.shape[0], boundary, int(const), None if sum_out is None else C.c_void_p(sum_out.data_ptr()),
+           None if max_out is None else C.c_void_p(max_out.data_ptr()), _stream(stream))
+    return out
+
+
+def gray(rgba, out=None, weights=(77, 150, 29), shift=8, stream=None):
+    if out is None:
+        out = torch.empty(rgba.shape[:-1], dtype=torch.uint8, device=rgba.device)
+    vi, vo = view(rgba, rgba=True), view(out)
+    L.call("hgb_point_gray", C.byref(vi), C.byref(vo), weights[0], weights[1], weights[2], shift, _stream(stream))
+    return out
+
+
+def binary(op, a, b, out=None, alpha=1.0, beta=1.0, stream=None):
+    if out is None:
+        out = torch.empty_like(a)
+    va, vb, vo = view(a), view(b), view(out)
+    L.call("hgb_point_binary", op, C.byref(va), C.byref(vb), C.byref(vo), float(alpha), float(beta),
+           _stream(stream))
+    return out
+
+
+def convert(inp, dtype, stream=None):
+    out = torch.empty(inp.shape, dtype=dtype, device=inp.device)
+    vi, vo = view(inp), view(out)
+    L.call("hgb_convert", C.byref(vi), C.byref(vo), _stream(stream))
+    return out
+
+
+def resample(inp, out, mode="lf", stream=None):
+    vi, vo = view(inp), view(out)
+    L.call("hgb_resample", C.byref(vi), C.byref(vo), 1 if mode == "nn" else 2, _stream(stream))
+    return out
+
+
+def reduce(inp, op=SUM, win=None, result_dev=None, stream=None):
+    """Global reduction; returns the host value (int for integer data, float for floats)."""
+    vi = view(inp)
+    host = C.create_string_buffer(8)
+    L.call("hgb_reduce", C.byref(vi), window(win), op,
+           None if result_dev is None else C.c_void_p(result_dev.data_ptr()), host, _stream(stream))
+    raw = host.raw
+    if inp.dtype in (torch.float32, torch.float16, torch.bfloat16, torch.float64):
+        return struct.unpack("<d", raw)[0]
+    if inp.dtype in (torch.int16, torch.int32) and op != SUM:
+        return struct.unpack("<q", raw)[0]
+    if inp.dtype in (torch.int16, torch.int32):
+        return struct.unpack("<q", raw)[0]
+    return struct.unpack("<Q", raw)[0]
+
+
+def separable(inp, out=None, row_taps=None, col_taps=None, boundary=CLAMP, const=0.0, stream=None):
+    if out is None:
+        out = torch.empty_like(inp)
+    r = np.ascontiguousarray(row_taps, np.float32)
+    c = np.ascontiguousarray(col_taps if col_taps is not None else row_taps, np.float32)
+    vi, vo = view(inp), view(out)
+    L.call("hgb_separable", C.byref(vi), C.byref(vo), r.ctypes.data_as(C.c_void_p), c.ctypes.data_as(C.c_void_p),
+           len(r), boundary, float(const), _stream(stream))
+    return out
+
+
+def bilateral(inp, out=None, smask=None, sigma_r=0.1, boundary=CLAMP, const=0.0, fast_weights=False, stream=None):
+    if out is None:
+        out = torch.empty_like(inp)
+    s = np.ascontiguousarray(smask, np.float32)
+    vi, vo = view(inp), view(out)
+    L.call("hgb_bilateral", C.byref(vi), C.byref(vo), s.ctypes.data_as(C.c_void_p), s.shape[0], float(sigma_r),
+           boundary, float(const), 1 if fast_weights else 0, _stream(stream))
+    return out
+
+
+def set_timing(on: bool) -> None:
+    L.call("hgb_set_timing", 1 if on else 0)
+
+
+def last_kernel_timing() -> float:
+    return float(L.load().hgb_last_kernel_timing())
+
+
+def autotune(on: bool) -> None:
+    L.call("hgb_autotune_enable", 1 if on else 0)

@@ -1,0 +1,191 @@
+// local_op.cuh -- local operator kernels (mask / domain stencils).
+//
+// Semantics: one output pixel of Hipacc's generated local-operator kernel
+// (lib/AST/ASTTranslate.cpp:510-1197): the mask is unrolled row-major
+// (lib/AST/Convolution.cpp:397-435) starting from get_init(mode)
+// (lib/AST/Convolution.cpp:90-100); every tap reads the accessor through the
+// boundary remap (lib/AST/BorderHandling.cpp:124-407).
+//
+// GB300 design: a CTA computes a TW x TH output tile.  Its input tile plus
+// halo is staged once in shared memory as FP32 with 16-byte global loads; only
+// the chunks that leave the accessor window are remapped element by element.
+// Each thread keeps a PX x PY block of outputs in registers and streams the
+// input rows of its column window through registers, so every staged value
+// feeds up to PX*MW*... FMAs.  SUM uses fused multiply-add in the row-major
+// tap order, which is the contracted form of the reference's `_tmp += m*x`.
+#pragma once
+
+#include "hgb_internal.cuh"
+
+namespace hgb {
+
+constexpr int kMaxMask = 15;
+
+struct ConvParams {
+  const char *in;
+  int64_t in_pitch, in_bstride;
+  char *out;
+  int64_t out_pitch, out_bstride;
+  int acc_ox, acc_oy, acc_w, acc_h;  // Accessor window (absolute, input)
+  int is_ox, is_oy, is_w, is_h;      // IterationSpace window (absolute, output)
+  int bmode;
+  float cval;
+  int vec_in, vec_out;               // 16-byte vector access legal
+  float mask[kMaxMask * kMaxMask];   // row-major, padded shape
+};
+
+struct TileCfg {
+  int bx, by, px, py;
+};
+
+// fast SUM-convolution kernels exist for these padded shapes
+constexpr int kFastSizes[] = {3, 5, 7, 9, 11, 13};
+
+template <typename TI, typename TO, int MW, int MH, int BX, int BY, int PX, int PY>
+__global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ ConvParams p) {
+  constexpr int NT = BX * BY;
+  constexpr int RX = MW / 2, RY = MH / 2;
+  constexpr int TW = BX * PX, TH = BY * PY;
+  constexpr int VI = Vec16<TI>::N;
+  constexpr int HL = round_up(RX, VI);
+  constexpr int HR = round_up(MW - 1 - RX, VI);
+  constexpr int SW = HL + TW + HR;
+  constexpr int SH = TH + MH - 1;
+  constexpr int CPR = SW / VI;
+  static_assert(TW % VI == 0 && SW % 4 == 0 && PX % 4 == 0, "tile shape");
+  __shared__ __align__(16) float tile[SH * SW];
+
+  const int b = blockIdx.z;
+  const int i0 = blockIdx.x * TW, j0 = blockIdx.y * TH;
+  const char *in = p.in + (int64_t)b * p.in_bstride;
+  const int X0 = p.acc_ox + i0 - HL;
+  const int Y0 = p.acc_oy + j0 - RY;
+  const int ax_lo = p.acc_ox, ax_hi = p.acc_ox + p.acc_w;
+  const int ay_lo = p.acc_oy, ay_hi = p.acc_oy + p.acc_h;
+
+  // ---- stage input tile + halo as FP32
+  const bool interior = X0 >= ax_lo && X0 + SW <= ax_hi && Y0 >= ay_lo && Y0 + SH <= ay_hi;
+  if (interior && p.vec_in) {
+#pragma unroll 4
+    for (int c = threadIdx.x; c < SH * CPR; c += NT) {
+      const int r = c / CPR, k = c - r * CPR;
+      const TI *src = reinterpret_cast<const TI *>(in + (int64_t)(Y0 + r) * p.in_pitch) + X0 + k * VI;
+      float f[VI];
+      Vec16<TI>::unpack(ldg16(src), f);
+      float *dst = &tile[r * SW + k * VI];
+#pragma unroll
+      for (int q = 0; q < VI; q += 4) *reinterpret_cast<float4 *>(dst + q) = make_float4(f[q], f[q + 1], f[q + 2], f[q + 3]);
+    }
+  } else {
+    for (int c = threadIdx.x; c < SH * CPR; c += NT) {
+      const int r = c / CPR, k = c - r * CPR;
+      const int ay = Y0 + r, ax0 = X0 + k * VI;
+      float f[VI];
+      if (p.vec_in && ay >= ay_lo && ay < ay_hi && ax0 >= ax_lo && ax0 + VI <= ax_hi) {
+        const TI *src = reinterpret_cast<const TI *>(in + (int64_t)ay * p.in_pitch) + ax0;
+        Vec16<TI>::unpack(ldg16(src), f);
+      } else {
+        const int ry = remap(p.bmode, ay, ay_lo, ay_hi);
+        const TI *row = reinterpret_cast<const TI *>(in + (int64_t)(ry == (int)0x80000000 ? ay_lo : ry) * p.in_pitch);
+#pragma unroll
+        for (int q = 0; q < VI; ++q) {
+          const int rx = remap(p.bmode, ax0 + q, ax_lo, ax_hi);
+          f[q] = (rx == (int)0x80000000 || ry == (int)0x80000000) ? p.cval : Storage<TI>::load(row + rx);
+        }
+      }
+      float *dst = &tile[r * SW + k * VI];
+#pragma unroll
+      for (int q = 0; q < VI; q += 4) *reinterpret_cast<float4 *>(dst + q) = make_float4(f[q], f[q + 1], f[q + 2], f[q + 3]);
+    }
+  }
+  __syncthreads();
+
+  // ---- register-blocked stencil
+  const int tx = threadIdx.x % BX, ty = threadIdx.x / BX;
+  constexpr int OFF = (HL - RX) % 4;
+  constexpr int NV = cdiv(OFF + PX + MW - 1, 4);
+  const int cbase = HL - RX - OFF + tx * PX;
+  float acc[PY][PX];
+#pragma unroll
+  for (int oy = 0; oy < PY; ++oy)
+#pragma unroll
+    for (int px = 0; px < PX; ++px) acc[oy][px] = 0.0f;
+
+#pragma unroll
+  for (int r = 0; r < PY + MH - 1; ++r) {
+    float win[NV * 4];
+    const float *row = &tile[(ty * PY + r) * SW + cbase];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const float4 t = *reinterpret_cast<const float4 *>(row + 4 * v);
+      win[4 * v] = t.x;
+      win[4 * v + 1] = t.y;
+      win[4 * v + 2] = t.z;
+      win[4 * v + 3] = t.w;
+    }
+#pragma unroll
+    for (int oy = 0; oy < PY; ++oy) {
+      const int my = r - oy;
+      if (my < 0 || my >= MH) continue;
+#pragma unroll
+      for (int px = 0; px < PX; ++px)
+#pragma unroll
+        for (int mx = 0; mx < MW; ++mx) acc[oy][px] = __fmaf_rn(p.mask[my * MW + mx], win[OFF + px + mx], acc[oy][px]);
+    }
+  }
+
+  // ---- store
+  char *out = p.out + (int64_t)b * p.out_bstride;
+  const int i = i0 + tx * PX;
+#pragma unroll
+  for (int oy = 0; oy < PY; ++oy) {
+    const int j = j0 + ty * PY + oy;
+    if (j >= p.is_h || i >= p.is_w) continue;
+    TO *dst = reinterpret_cast<TO *>(out + (int64_t)(p.is_oy + j) * p.out_pitch) + p.is_ox + i;
+    if (p.vec_out && i + PX <= p.is_w) {
+      if constexpr (sizeof(TO) == 4) {
+#pragma unroll
+        for (int q = 0; q < PX; q += 4)
+          *reinterpret_cast<float4 *>(dst + q) = make_float4(acc[oy][q], acc[oy][q + 1], acc[oy][q + 2], acc[oy][q + 3]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < PX; q += 4) {
+          TO t4[4] = {Storage<TO>::from_f(acc[oy][q]), Storage<TO>::from_f(acc[oy][q + 1]),
+                      Storage<TO>::from_f(acc[oy][q + 2]), Storage<TO>::from_f(acc[oy][q + 3])};
+          *reinterpret_cast<uint2 *>(dst + q) = *reinterpret_cast<const uint2 *>(t4);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int px = 0; px < PX; ++px)
+        if (i + px < p.is_w) dst[px] = Storage<TO>::from_f(acc[oy][px]);
+    }
+  }
+}
+
+// General path: any mask shape up to 15x15, any reduce mode, optional domain,
+// mask from host parameters or from device memory.  One output per thread.
+struct GenParams {
+  ConvParams c;
+  int mw, mh, reduce;
+  int has_mask;
+  const float *mask_dev;
+  uint8_t domain[kMaxMask * kMaxMask];
+};
+
+template <typename TI, typename TO>
+int launch_conv_square(const ConvParams &p, int mw, int mh, int batch, cudaStream_t st, int cfg_index);
+template <typename TI, typename TO>
+int launch_conv_line(const ConvParams &p, int mw, int mh, int batch, cudaStream_t st, int cfg_index);
+template <typename TI, typename TO>
+int launch_conv(const ConvParams &p, int mw, int mh, int batch, cudaStream_t st, int cfg_index) {
+  return (mw == mh) ? launch_conv_square<TI, TO>(p, mw, mh, batch, st, cfg_index)
+                    : launch_conv_line<TI, TO>(p, mw, mh, batch, st, cfg_index);
+}
+template <typename TI, typename TO>
+int launch_generic(const GenParams &p, int batch, cudaStream_t st);
+
+int num_tile_cfgs();
+TileCfg tile_cfg(int i);
+
+}  // namespace hgb

@@ -1,0 +1,6 @@
+// lop_line_bf16.cu -- line local-operator kernels for bf16 storage (local_op.cuh).
+#include "local_op_kernels.cuh"
+
+namespace hgb {
+HGB_INSTANTIATE_LINE(__nv_bfloat16, __nv_bfloat16)
+}  // namespace hgb

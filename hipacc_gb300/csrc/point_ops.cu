@@ -1,0 +1,320 @@
+// point_ops.cu -- point operators: RGBA->gray, binary combinations, storage
+// conversion and resampling reads.
+//
+// Point operators in the reference are generated per kernel with one pixel
+// per thread and scalar loads (lib/AST/ASTTranslate.cpp:923, pixels per thread
+// from include/hipacc/Device/TargetDescription.h:85-91).  Here every thread
+// moves 16 pixels with 16-byte vector loads and stores over a grid sized to
+// the SM count; dense images are treated as one long row.
+#include "hgb_internal.cuh"
+
+namespace hgb {
+namespace {
+
+struct RowSpace {
+  // iteration over (batch, row, chunk-of-16) work items; dense images fold
+  // into a single row per image
+  int rows_per_img, row_len, chunks_per_row;
+  int64_t nitems;
+};
+
+RowSpace make_rows(int w, int h, int batch, bool dense) {
+  RowSpace r;
+  if (dense) {
+    r.rows_per_img = 1;
+    r.row_len = w * h;
+  } else {
+    r.rows_per_img = h;
+    r.row_len = w;
+  }
+  r.chunks_per_row = cdiv(r.row_len, 16);
+  r.nitems = (int64_t)batch * r.rows_per_img * r.chunks_per_row;
+  return r;
+}
+
+int grid_for(int64_t items, int threads) {
+  const int64_t need = (items + threads - 1) / threads;
+  const int64_t cap = (int64_t)num_sms() * 8;
+  return (int)(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
+struct GrayParams {
+  const uint8_t *in;
+  int64_t in_pitch, in_bstride;
+  uint8_t *out;
+  int64_t out_pitch, out_bstride;
+  RowSpace rs;
+  int vec;
+  uint32_t wpack;  // wr | wg << 8 | wb << 16 when every weight fits a byte
+  int wr, wg, wb, shift, use_dp4a;
+};
+
+__device__ __forceinline__ uint32_t gray_px(const GrayParams &p, uint32_t rgba) {
+  uint32_t v;
+  if (p.use_dp4a)
+    v = __dp4a(rgba, p.wpack, 0u);
+  else
+    v = (uint32_t)(p.wr * (int)(rgba & 0xff) + p.wg * (int)((rgba >> 8) & 0xff) + p.wb * (int)((rgba >> 16) & 0xff));
+  return (v >> p.shift) & 0xffu;
+}
+
+__global__ void __launch_bounds__(256) gray_kernel(const __grid_constant__ GrayParams p) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < p.rs.nitems; it += stride) {
+    const int chunk = (int)(it % p.rs.chunks_per_row);
+    const int64_t row_g = it / p.rs.chunks_per_row;
+    const int b = (int)(row_g / p.rs.rows_per_img);
+    const int row = (int)(row_g - (int64_t)b * p.rs.rows_per_img);
+    const uint8_t *src = p.in + (int64_t)b * p.in_bstride + (int64_t)row * p.in_pitch + (int64_t)chunk * 64;
+    uint8_t *dst = p.out + (int64_t)b * p.out_bstride + (int64_t)row * p.out_pitch + (int64_t)chunk * 16;
+    const int x0 = chunk * 16;
+    if (p.vec && x0 + 16 <= p.rs.row_len) {
+      uint4 a = ldg16(src), bq = ldg16(src + 16), c = ldg16(src + 32), d = ldg16(src + 48);
+      const uint32_t px[16] = {a.x, a.y, a.z, a.w, bq.x, bq.y, bq.z, bq.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
+      uint32_t o[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        o[q] = gray_px(p, px[4 * q]) | (gray_px(p, px[4 * q + 1]) << 8) | (gray_px(p, px[4 * q + 2]) << 16) |
+               (gray_px(p, px[4 * q + 3]) << 24);
+      stg16(dst, make_uint4(o[0], o[1], o[2], o[3]));
+    } else {
+      for (int q = 0; q < 16 && x0 + q < p.rs.row_len; ++q) {
+        const uint8_t *s = src + 4 * q;
+        const uint32_t rgba = (uint32_t)s[0] | ((uint32_t)s[1] << 8) | ((uint32_t)s[2] << 16) | ((uint32_t)s[3] << 24);
+        dst[q] = (uint8_t)gray_px(p, rgba);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- binary ops
+template <typename T>
+struct BinParams {
+  const char *a, *b;
+  char *out;
+  int64_t a_pitch, b_pitch, o_pitch, a_bs, b_bs, o_bs;
+  RowSpace rs;
+  int op;
+  float alpha, beta;
+};
+
+template <typename T>
+__device__ __forceinline__ float bin_apply(const BinParams<T> &p, float a, float b) {
+  switch (p.op) {
+    case 0: return __fsub_rn(a, b);
+    case 1: return __fadd_rn(a, b);
+    default: return __fadd_rn(__fmul_rn(p.alpha, a), __fmul_rn(p.beta, b));
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) binary_kernel(const __grid_constant__ BinParams<T> p) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < p.rs.nitems; it += stride) {
+    const int chunk = (int)(it % p.rs.chunks_per_row);
+    const int64_t row_g = it / p.rs.chunks_per_row;
+    const int bi = (int)(row_g / p.rs.rows_per_img);
+    const int row = (int)(row_g - (int64_t)bi * p.rs.rows_per_img);
+    const T *a = reinterpret_cast<const T *>(p.a + bi * p.a_bs + row * p.a_pitch) + chunk * 16;
+    const T *b = reinterpret_cast<const T *>(p.b + bi * p.b_bs + row * p.b_pitch) + chunk * 16;
+    T *o = reinterpret_cast<T *>(p.out + bi * p.o_bs + row * p.o_pitch) + chunk * 16;
+    const int x0 = chunk * 16;
+    for (int q = 0; q < 16 && x0 + q < p.rs.row_len; ++q)
+      o[q] = Storage<T>::from_f(bin_apply(p, Storage<T>::to_f(a[q]), Storage<T>::to_f(b[q])));
+  }
+}
+
+// ---------------------------------------------------------------- convert
+template <typename TI, typename TO>
+__global__ void __launch_bounds__(256) convert_kernel(const char *in, int64_t ip, int64_t ibs, char *out, int64_t op,
+                                                      int64_t obs, int w, int h, int batch) {
+  const int64_t n = (int64_t)w * h * batch;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int x = (int)(i % w);
+    const int64_t r = i / w;
+    const int y = (int)(r % h), b = (int)(r / h);
+    const TI v = reinterpret_cast<const TI *>(in + b * ibs + y * ip)[x];
+    float f;
+    if constexpr (sizeof(TI) == 1)
+      f = (float)v;
+    else
+      f = Storage<TI>::to_f(v);
+    TO *o = reinterpret_cast<TO *>(out + b * obs + y * op) + x;
+    if constexpr (sizeof(TO) == 1) {
+      // truncation toward zero as a C cast, saturated to [0, 255]
+      f = fminf(fmaxf(f, 0.0f), 255.0f);
+      *o = (TO)(int)f;
+    } else {
+      *o = Storage<TO>::from_f(f);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- resample
+// lib/AST/Interpolate.cpp:85-113 (mapped = scale/2 + scale*x, contracted to
+// one fma as nvcc and aarch64 GCC do) and runtime/hipacc_cu_interpolate.hpp:173-216.
+__device__ __forceinline__ float mapped(float s, int x) { return __fmaf_rn(s, (float)x, s * 0.5f); }
+
+__device__ __forceinline__ float lf_sample(const float *src, int64_t sp, int sw, int sh, float xm, float ym) {
+  float xb = xm - 0.5f, yb = ym - 0.5f;
+  xb = xb < 0.0f ? 0.0f : xb;
+  yb = yb < 0.0f ? 0.0f : yb;
+  const int xi = (int)xb, yi = (int)yb;
+  const float xf = xb - (float)xi, yf = yb - (float)yi;
+  const int x0 = min(xi, sw - 1), x1 = min(xi + 1, sw - 1), y0 = min(yi, sh - 1), y1 = min(yi + 1, sh - 1);
+  const float *r0 = reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + y0 * sp);
+  const float *r1 = reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + y1 * sp);
+  const float wa = __fmul_rn(1.0f - xf, 1.0f - yf), wb = __fmul_rn(xf, 1.0f - yf);
+  const float wc = __fmul_rn(1.0f - xf, yf), wd = __fmul_rn(xf, yf);
+  float r = __fmul_rn(wa, __ldg(r0 + x0));
+  r = __fmaf_rn(wb, __ldg(r0 + x1), r);
+  r = __fmaf_rn(wc, __ldg(r1 + x0), r);
+  r = __fmaf_rn(wd, __ldg(r1 + x1), r);
+  return r;
+}
+
+__global__ void __launch_bounds__(256) resample_kernel(const char *in, int64_t ip, int64_t ibs, int sw, int sh,
+                                                       char *out, int64_t op, int64_t obs, int dw, int dh, int batch,
+                                                       int imode) {
+  const float sx = (float)sw / (float)dw, sy = (float)sh / (float)dh;
+  const int64_t n = (int64_t)dw * dh * batch;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int x = (int)(i % dw);
+    const int64_t r = i / dw;
+    const int y = (int)(r % dh), b = (int)(r / dh);
+    const float *src = reinterpret_cast<const float *>(in + b * ibs);
+    float v;
+    if (imode == 1) {
+      int xx = (int)mapped(sx, x), yy = (int)mapped(sy, y);
+      xx = min(max(xx, 0), sw - 1);
+      yy = min(max(yy, 0), sh - 1);
+      v = __ldg(reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + yy * ip) + xx);
+    } else {
+      v = lf_sample(src, ip, sw, sh, mapped(sx, x), mapped(sy, y));
+    }
+    reinterpret_cast<float *>(out + b * obs + y * op)[x] = v;
+  }
+}
+
+bool dense(const hgb_view &v) {
+  const int64_t row = (int64_t)v.width * dtype_size(v.dtype);
+  return v.pitch == row && (v.batch == 1 || v.batch_stride == row * v.height);
+}
+
+}  // namespace
+}  // namespace hgb
+
+using namespace hgb;
+
+extern "C" int hgb_point_gray(const hgb_view *in, const hgb_view *out, int wr, int wg, int wb, int shift, void *stream) {
+  int rc = check_view(in, "in");
+  if (rc) return rc;
+  rc = check_view(out, "out");
+  if (rc) return rc;
+  HGB_REQUIRE(in->dtype == HGB_U8X4 && out->dtype == HGB_U8, "hgb_point_gray: uchar4 -> u8 expected");
+  HGB_REQUIRE(in->width == out->width && in->height == out->height && in->batch == out->batch,
+              "hgb_point_gray: size mismatch");
+  HGB_REQUIRE(wr >= 0 && wg >= 0 && wb >= 0 && shift >= 0 && shift < 32 && wr + wg + wb < (1 << 23),
+              "hgb_point_gray: bad weights");
+  GrayParams p;
+  p.in = (const uint8_t *)in->data;
+  p.in_pitch = in->pitch;
+  p.in_bstride = in->batch_stride;
+  p.out = (uint8_t *)out->data;
+  p.out_pitch = out->pitch;
+  p.out_bstride = out->batch_stride;
+  const bool d = dense(*in) && dense(*out);
+  p.rs = make_rows(in->width, in->height, in->batch, d);
+  // vector path: every chunk start is 16-byte aligned on both sides
+  p.vec = ((uintptr_t)in->data % 16 == 0) && ((uintptr_t)out->data % 16 == 0) &&
+          (d || (in->pitch % 16 == 0 && out->pitch % 16 == 0)) &&
+          (in->batch == 1 || (in->batch_stride % 16 == 0 && out->batch_stride % 16 == 0));
+  p.wr = wr;
+  p.wg = wg;
+  p.wb = wb;
+  p.shift = shift;
+  p.use_dp4a = wr < 256 && wg < 256 && wb < 256;
+  p.wpack = (uint32_t)wr | ((uint32_t)wg << 8) | ((uint32_t)wb << 16);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t ev = before_launch(st);
+  gray_kernel<<<grid_for(p.rs.nitems, 256), 256, 0, st>>>(p);
+  return after_launch("gray_kernel", st, ev);
+}
+
+extern "C" int hgb_point_binary(int op, const hgb_view *a, const hgb_view *b, const hgb_view *out, float alpha,
+                                float beta, void *stream) {
+  int rc = check_view(a, "a");
+  if (rc) return rc;
+  rc = check_view(b, "b");
+  if (rc) return rc;
+  rc = check_view(out, "out");
+  if (rc) return rc;
+  HGB_REQUIRE(op >= 0 && op <= 2, "hgb_point_binary: bad op");
+  HGB_REQUIRE(a->dtype == b->dtype && a->dtype == out->dtype && is_float_storage(a->dtype),
+              "hgb_point_binary: same float storage expected");
+  HGB_REQUIRE(a->width == out->width && b->width == out->width && a->height == out->height &&
+                  b->height == out->height && a->batch == out->batch && b->batch == out->batch,
+              "hgb_point_binary: size mismatch");
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool d = dense(*a) && dense(*b) && dense(*out);
+  cudaEvent_t ev = before_launch(st);
+#define HGB_BIN(T)                                                                                              \
+  {                                                                                                             \
+    BinParams<T> p{(const char *)a->data, (const char *)b->data, (char *)out->data, a->pitch, b->pitch,         \
+                   out->pitch, a->batch_stride, b->batch_stride, out->batch_stride,                             \
+                   make_rows(a->width, a->height, a->batch, d), op, alpha, beta};                               \
+    binary_kernel<T><<<grid_for(p.rs.nitems, 256), 256, 0, st>>>(p);                                           \
+  }
+  if (a->dtype == HGB_F32) HGB_BIN(float) else if (a->dtype == HGB_BF16) HGB_BIN(__nv_bfloat16) else HGB_BIN(__half)
+#undef HGB_BIN
+  return after_launch("binary_kernel", st, ev);
+}
+
+extern "C" int hgb_convert(const hgb_view *in, const hgb_view *out, void *stream) {
+  int rc = check_view(in, "in");
+  if (rc) return rc;
+  rc = check_view(out, "out");
+  if (rc) return rc;
+  HGB_REQUIRE(in->width == out->width && in->height == out->height && in->batch == out->batch,
+              "hgb_convert: size mismatch");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t n = (int64_t)in->width * in->height * in->batch;
+  const int grid = grid_for(n, 256);
+  cudaEvent_t ev = before_launch(st);
+#define HGB_CV(TI, TO) \
+  convert_kernel<TI, TO><<<grid, 256, 0, st>>>((const char *)in->data, in->pitch, in->batch_stride, (char *)out->data, \
+                                               out->pitch, out->batch_stride, in->width, in->height, in->batch)
+  const int a = in->dtype, b = out->dtype;
+  if (a == HGB_F32 && b == HGB_BF16) HGB_CV(float, __nv_bfloat16);
+  else if (a == HGB_F32 && b == HGB_F16) HGB_CV(float, __half);
+  else if (a == HGB_BF16 && b == HGB_F32) HGB_CV(__nv_bfloat16, float);
+  else if (a == HGB_F16 && b == HGB_F32) HGB_CV(__half, float);
+  else if (a == HGB_F32 && b == HGB_F32) HGB_CV(float, float);
+  else if (a == HGB_U8 && b == HGB_F32) HGB_CV(uint8_t, float);
+  else if (a == HGB_F32 && b == HGB_U8) HGB_CV(float, uint8_t);
+  else {
+    if (ev) cudaEventDestroy(ev);
+    return set_error(HGB_ERR_UNSUPPORTED, "hgb_convert: unsupported dtype pair");
+  }
+#undef HGB_CV
+  return after_launch("convert_kernel", st, ev);
+}
+
+extern "C" int hgb_resample(const hgb_view *in, const hgb_view *out, int imode, void *stream) {
+  int rc = check_view(in, "in");
+  if (rc) return rc;
+  rc = check_view(out, "out");
+  if (rc) return rc;
+  HGB_REQUIRE(in->dtype == HGB_F32 && out->dtype == HGB_F32, "hgb_resample: f32 expected");
+  HGB_REQUIRE(imode == 1 || imode == 2, "hgb_resample: imode must be 1 (NN) or 2 (LF)");
+  HGB_REQUIRE(in->batch == out->batch, "hgb_resample: batch mismatch");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t n = (int64_t)out->width * out->height * out->batch;
+  cudaEvent_t ev = before_launch(st);
+  resample_kernel<<<grid_for(n, 256), 256, 0, st>>>((const char *)in->data, in->pitch, in->batch_stride, in->width,
+                                                    in->height, (char *)out->data, out->pitch, out->batch_stride,
+                                                    out->width, out->height, out->batch, imode);
+  return after_launch("resample_kernel", st, ev);
+}

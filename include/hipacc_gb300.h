@@ -1,0 +1,285 @@
+/*
+ * hipacc_gb300.h -- C ABI of libhipacc_gb300.so, the GB300 (sm_103a) kernels
+ * for the image-processing hot path of Hipacc's generated code: local
+ * operators, point operators, global reductions and pyramid construction,
+ * plus reduced-precision storage, batched/persistent pyramid launches and
+ * adjoint kernels.
+ *
+ * Every entry point returns an int status (HGB_OK = 0) and records a
+ * thread-local message readable with hgb_last_error().  Nothing aborts the
+ * process and no kernel traps: device-side failures (bounded-wait timeouts)
+ * come back as HGB_ERR_TIMEOUT.  Pointers named *_dev are device addresses;
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  All launches are
+ * asynchronous unless a host result is requested.
+ *
+ * The comment above each entry point names the reference interface it
+ * replaces (paths inside the Hipacc source tree).
+ */
+#ifndef HIPACC_GB300_H
+#define HIPACC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HGB_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define HGB_API __attribute__((visibility("default")))
+#else
+#define HGB_API
+#endif
+
+typedef enum hgb_status {
+  HGB_OK = 0,
+  HGB_ERR_INVALID = 1,     /* bad argument: null pointer, size, dtype, window */
+  HGB_ERR_UNSUPPORTED = 2, /* valid request this build has no kernel for */
+  HGB_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  HGB_ERR_ALLOC = 4,       /* device or host allocation failed */
+  HGB_ERR_TIMEOUT = 5,     /* a bounded device-side wait expired */
+  HGB_ERR_LIMIT = 6        /* request exceeds a fixed capacity */
+} hgb_status;
+
+/* pixel storage types */
+typedef enum hgb_dtype {
+  HGB_U8 = 0,
+  HGB_U8X4 = 1, /* uchar4, RGBA */
+  HGB_I16 = 2,
+  HGB_U16 = 3,
+  HGB_I32 = 4,
+  HGB_U32 = 5,
+  HGB_U64 = 6,
+  HGB_F16 = 7,
+  HGB_BF16 = 8,
+  HGB_F32 = 9,
+  HGB_F64 = 10
+} hgb_dtype;
+
+/* hipacc::Boundary numbering (dsl/image.hpp:46-52) */
+typedef enum hgb_boundary {
+  HGB_BOUNDARY_UNDEFINED = 0,
+  HGB_BOUNDARY_CLAMP = 1,
+  HGB_BOUNDARY_REPEAT = 2,
+  HGB_BOUNDARY_MIRROR = 3,
+  HGB_BOUNDARY_CONSTANT = 4
+} hgb_boundary;
+
+/* hipacc::Reduce numbering (dsl/kernel.hpp:48-54); MEDIAN is not implemented
+ * by the reference either */
+typedef enum hgb_reduce_op { HGB_REDUCE_SUM = 0, HGB_REDUCE_MIN = 1, HGB_REDUCE_MAX = 2, HGB_REDUCE_PROD = 3 } hgb_reduce_op;
+
+/* A device image or a batch of equally sized device images.
+ * Replaces HipaccImageCudaRaw<T> (runtime/hipacc_cu.hpp:113-160): stride is in
+ * bytes here and a batch dimension is added. */
+typedef struct hgb_view {
+  void *data;           /* device address of pixel (0,0) of image 0 */
+  int32_t dtype;        /* hgb_dtype */
+  int32_t width;        /* pixels */
+  int32_t height;       /* rows */
+  int32_t batch;        /* images, >= 1 */
+  int64_t pitch;        /* bytes between rows */
+  int64_t batch_stride; /* bytes between images (ignored when batch == 1) */
+} hgb_view;
+
+/* Accessor window / IterationSpace ROI (HipaccAccessorBase,
+ * runtime/hipacc_base.hpp:76-85; IterationSpace, dsl/iterationspace.hpp:118-133).
+ * A NULL window means the whole image. */
+typedef struct hgb_window {
+  int32_t offset_x, offset_y, width, height;
+} hgb_window;
+
+/* ------------------------------------------------------------------ */
+/* runtime                                                             */
+/* ------------------------------------------------------------------ */
+
+/* Library ABI version (HGB_ABI_VERSION of the build). */
+HGB_API int hgb_abi_version(void);
+
+/* hipaccInitCUDA (runtime/hipacc_cu_standalone.hpp:113-163): select the
+ * device, create its context and report its name into `name` (may be NULL). */
+HGB_API int hgb_init(int device, char *name, size_t name_len);
+
+/* Message of the last failing call on this thread ("" if none). */
+HGB_API const char *hgb_last_error(void);
+
+/* -time-kernels / hipacc_last_kernel_timing (runtime/hipacc_base.hpp:54-66,
+ * runtime/hipacc_cu_standalone.hpp:297-326): when on, every launch is
+ * bracketed by CUDA events on its stream and synchronised; the duration in ms
+ * is kept per thread. */
+HGB_API int hgb_set_timing(int on);
+HGB_API float hgb_last_kernel_timing(void);
+
+/* Tile-configuration autotuning (replaces the compile-time -use-config /
+ * -pixels-per-thread choices, include/hipacc/Device/TargetDescription.h:53-191):
+ * when enabled, the first call of an operator for a new shape class times
+ * each tile configuration and keeps the fastest; choices persist as JSON. */
+HGB_API int hgb_autotune_enable(int on);
+HGB_API int hgb_autotune_clear(void);
+HGB_API int hgb_autotune_count(void);
+HGB_API int hgb_autotune_save(const char *path);
+HGB_API int hgb_autotune_load(const char *path);
+
+/* Reserve the per-device workspace (reduction partials, tickets, work-lists)
+ * up front, e.g. before stream capture.  Calls grow it on demand otherwise. */
+HGB_API int hgb_workspace_reserve(size_t bytes);
+
+/* Image memory: hipaccCreateMemory<T> (runtime/hipacc_cu.tpp:50-81, row pitch
+ * rounded up to `alignment` bytes, 0 = 256), hipaccWriteMemory (84-116),
+ * hipaccReadMemory (165-193), hipaccCopyMemory / hipaccCopyMemoryRegion
+ * (runtime/hipacc_cu_standalone.hpp:165-216).  `host` buffers are dense rows
+ * of width * element size bytes. */
+typedef struct hgb_image hgb_image;
+HGB_API int hgb_image_create(int dtype, int width, int height, int alignment, const void *host_init, hgb_image **out);
+HGB_API int hgb_image_destroy(hgb_image *img);
+HGB_API int hgb_image_get_view(const hgb_image *img, hgb_view *out);
+HGB_API int hgb_image_write(hgb_image *img, const void *host, void *stream);
+HGB_API int hgb_image_read(const hgb_image *img, void *host, void *stream);
+HGB_API int hgb_image_copy(const hgb_image *src, hgb_image *dst, void *stream);
+HGB_API int hgb_image_copy_region(const hgb_image *src, const hgb_window *src_win, hgb_image *dst,
+                          const hgb_window *dst_win, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* local operators                                                     */
+/* ------------------------------------------------------------------ */
+
+/* One generated local-operator kernel (lib/AST/ASTTranslate.cpp:510-1197,
+ * launched by hipaccLaunchKernel, runtime/hipacc_cu_standalone.hpp:277-329):
+ *   out(is) = fold_{mask cells c} reduce(init, mask[c] * in(acc + c))
+ * Kernel::convolve (dsl/kernel.hpp:241-267) when `mask` is set, and
+ * Kernel::reduce(Domain) (dsl/kernel.hpp:270-296) over `domain` (non-zero
+ * cells) otherwise; both may be given (mask(dom) * input(dom)).  The fold is
+ * row-major from get_init(reduce) (lib/AST/Convolution.cpp:90-100), SUM as
+ * fused multiply-add.  Boundary remap per lib/AST/BorderHandling.cpp:41-407.
+ * in/out: f32, bf16 or f16 storage (same or different), FP32 arithmetic.
+ * mask_w, mask_h <= 15; `mask` / `domain` are host arrays (mask_h rows of
+ * mask_w); `mask_dev` (may replace `mask`) is a device array read at launch.
+ * in->batch == out->batch images are processed in one launch. */
+HGB_API int hgb_local_op(const hgb_view *in, const hgb_window *acc, const hgb_view *out, const hgb_window *iter,
+                 const float *mask, const float *mask_dev, const uint8_t *domain, int mask_w, int mask_h,
+                 int reduce, int boundary, float const_val, void *stream);
+
+/* Separable local operator: the reference writes it as two local operators
+ * with a 1xK and a Kx1 mask and an intermediate image; here one kernel keeps
+ * the row pass in shared memory (FP32), which gives the FP32 two-pass result
+ * bit for bit.  K <= 15, odd. */
+HGB_API int hgb_separable(const hgb_view *in, const hgb_view *out, const float *row_taps, const float *col_taps, int k,
+                  int boundary, float const_val, void *stream);
+
+/* Bilateral filter (samples-public/3_Preprocessing/Bilateral_Filter/src/main.cpp:63-77):
+ * out = sum s*in / sum s, s = exp(-c_r (in - centre)^2) * smask, c_r = 0.5/sigma_r^2.
+ * size odd <= 13.  flags bit 0: compute the range weights with packed half
+ * precision exponentials (f16/bf16 storage only; error stated by the tests). */
+HGB_API int hgb_bilateral(const hgb_view *in, const hgb_view *out, const float *smask, int size, float sigma_r,
+                  int boundary, float const_val, int flags, void *stream);
+
+/* Sobel magnitude min(|gx|+|gy|, 255) over u8 with the two integer masks'
+ * Domains (samples-public/3_Preprocessing/Sobel/src/main.cpp:56-67), with the
+ * global reductions of the result fused into the same kernel: the u64 sum and
+ * u8 max land in sum_dev / max_dev (either may be NULL).  size 3, 5 or 7. */
+HGB_API int hgb_sobel_mag(const hgb_view *in, const hgb_view *out, const int *mask_x, const int *mask_y, int size,
+                  int boundary, int const_val, uint64_t *sum_dev, uint32_t *max_dev, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* point operators                                                     */
+/* ------------------------------------------------------------------ */
+
+/* uchar4 -> uchar gray (samples-public/0_Point_Operators/Color_Conversion,
+ * integer form): out = (wr*R + wg*G + wb*B) >> shift, 16-byte vector I/O. */
+HGB_API int hgb_point_gray(const hgb_view *in, const hgb_view *out, int wr, int wg, int wb, int shift, void *stream);
+
+/* Element-wise combination of two images of the same size (the
+ * DifferenceOfGaussian / Restore point kernels,
+ * samples-public/5_Other/Gaussian_Laplacian_Pyramid/src/main.cpp:74-107):
+ * op 0: out = a - b, 1: out = a + b, 2: out = alpha*a + beta*b.  Float storage. */
+HGB_API int hgb_point_binary(int op, const hgb_view *a, const hgb_view *b, const hgb_view *out, float alpha, float beta,
+                     void *stream);
+
+/* Storage conversion between f32, bf16, f16 (round to nearest even) and u8. */
+HGB_API int hgb_convert(const hgb_view *in, const hgb_view *out, void *stream);
+
+/* Resampling accessor read as a point operator (Interpolate::NN / LF,
+ * lib/AST/Interpolate.cpp:85-113, runtime/hipacc_cu_interpolate.hpp:173-216):
+ * out(x,y) = in at the mapped position, CLAMP taps.  imode 1 = NN, 2 = LF. */
+HGB_API int hgb_resample(const hgb_view *in, const hgb_view *out, int imode, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* global reductions                                                   */
+/* ------------------------------------------------------------------ */
+
+/* Kernel::reduced_data (dsl/kernel.hpp:121-161) /
+ * hipaccApplyReductionShared (runtime/hipacc_cu.tpp:312-408): one pass over
+ * `in` (window may be NULL) with warp shuffles, a block combine and a
+ * last-block combine behind a release/acquire ticket.  Result types:
+ *   u8/u16/u32 SUM -> uint64, MIN/MAX -> same width as input (stored in a u32/u64 slot)
+ *   i16/i32 SUM -> int64;  u64 SUM -> uint64
+ *   f32 SUM -> per-thread Kahan partials, FP64 cross-block combine; result_dev
+ *   receives a double (the float result is its rounding);  f32 MIN/MAX/PROD -> float
+ *   f64 -> double
+ * `result_dev` (device, 8 bytes) and/or `result_host` (8 bytes; the call then
+ * synchronises the stream). */
+HGB_API int hgb_reduce(const hgb_view *in, const hgb_window *win, int op, void *result_dev, void *result_host,
+               void *stream);
+
+/* ------------------------------------------------------------------ */
+/* pyramids (Pyramid / traverse, dsl/pyramid.hpp:97-318;                */
+/* hipaccCreatePyramid, runtime/hipacc_cu.tpp:466-497)                  */
+/* ------------------------------------------------------------------ */
+
+/* A plan for the Laplacian pyramids of `n_images` FP32 images of uneven
+ * sizes: level l is floor(w / 2^l) x floor(h / 2^l) (dsl/pyramid.hpp:103-114),
+ * reduce = 5x5 mask + nearest-neighbour 2x downsample, expand = linear
+ * filtering upsample, as the Gaussian_Laplacian_Pyramid sample.  The plan
+ * owns the device arena of all levels and the tile work-list. */
+typedef struct hgb_pyramid_plan hgb_pyramid_plan;
+HGB_API int hgb_pyramid_plan_create(int n_images, const int *widths, const int *heights, int levels, const float *mask5,
+                            int boundary, hgb_pyramid_plan **out);
+HGB_API int hgb_pyramid_plan_destroy(hgb_pyramid_plan *plan);
+/* Device views of level `level` of image `image`: Gaussian G_l and
+ * Laplacian L_l (L of the last level is not defined; G of level 0 is the input
+ * slot the caller fills). */
+HGB_API int hgb_pyramid_level_view(const hgb_pyramid_plan *plan, int image, int level, hgb_view *gauss, hgb_view *lap);
+/* Build all levels of all images.  mode 0: one persistent launch over the tile
+ * work-list with bounded inter-level waits; mode 1: one launch per level over
+ * all images; mode 2: per image, per level plain launches (blur, subsample,
+ * difference), the reference's launch structure. */
+HGB_API int hgb_pyramid_decompose(hgb_pyramid_plan *plan, int mode, void *stream);
+/* Collapse (Restore): G_l = LF(G_{l+1}) + L_l from the bottom level up,
+ * into the plan's Gaussian levels. */
+HGB_API int hgb_pyramid_collapse(hgb_pyramid_plan *plan, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* adjoints                                                            */
+/* ------------------------------------------------------------------ */
+
+/* Adjoint of the SUM local operator out = conv(in, mask) with the boundary
+ * transposed: CLAMP/MIRROR/REPEAT gather every output that read a pixel
+ * through the remap, CONSTANT taps carry no gradient.
+ *   grad_in  (may be NULL) = conv^T(grad_out)
+ *   grad_mask_dev (may be NULL, mask_w*mask_h floats) = sum_p grad_out(p) * in(remap(p+c)),
+ *   deterministic: block partials combined in FP64 in a fixed order.
+ * mask is a device array (mask_dev) or host array (mask). */
+HGB_API int hgb_local_op_adjoint(const hgb_view *in, const hgb_view *grad_out, const hgb_view *grad_in, const float *mask,
+                         const float *mask_dev, int mask_w, int mask_h, int boundary, float *grad_mask_dev,
+                         void *stream);
+
+/* Forward + adjoint of the differentiation workload
+ *   y1 = conv(x, mask), y = bilateral(y1; smask, sigma_r), loss = mean((y - t)^2)
+ * in two fused kernels (forward with the loss gradient in its epilogue;
+ * adjoint of the bilateral and of the convolution with the bilateral weights
+ * recomputed).  x, t, grad_x: f32 batch views of the same size.  mask_dev and
+ * sigma_dev are device parameters; outputs: loss_dev (double), grad_x,
+ * grad_mask_dev (mask_k^2 floats), grad_sigma_dev (float).  mode 0 = fused,
+ * mode 1 = the unfused chain of plain kernels (for comparison). */
+HGB_API int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, const float *mask_dev, int mask_k,
+                           const float *smask, int smask_k, const float *sigma_dev, int boundary, int mode,
+                           double *loss_dev, const hgb_view *grad_x, float *grad_mask_dev, float *grad_sigma_dev,
+                           void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HIPACC_GB300_H */

@@ -1,0 +1,109 @@
+"""Generate tests/golden/*.npz from the reference's own DSL headers.
+
+Run in a tree where the reference sources exist (the oracle Makefile's `ref`
+target compiles dsl/*.hpp and runtime/hipacc_cpu_red.hpp of the reference as-is
+into oracle/_ref/libhgb_ref.so).  Every fixture holds the seeded inputs and the
+outputs the reference computed; tests/test_oracle_golden.py checks the
+restated oracle against them wherever the reference tree is absent.
+
+DSL mode ignores the CONSTANT value (dsl/image.hpp:260-291), so CONSTANT
+fixtures use the constant 0, where both agree.  Floating-point fixtures are
+compiled with -ffp-contract=off (no fused multiply-add).
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
+import oracle as O  # noqa: E402
+
+
+def main():
+    O.build()
+    R = O.ref()
+    if R is None:
+        raise SystemExit("oracle/_ref/libhgb_ref.so is not built (needs the reference tree)")
+    rng = np.random.default_rng(20261203)
+    out = {}
+
+    # local operators: Kernel::convolve with a Mask, all boundary modes
+    for (mh, mw) in [(3, 3), (5, 5), (1, 9), (9, 1), (13, 13)]:
+        for b in (O.CLAMP, O.REPEAT, O.MIRROR, O.CONSTANT):
+            h, w = 19, 23
+            img = rng.random((h, w), dtype=np.float32)
+            m = rng.random((mh, mw)).astype(np.float32)
+            r = np.zeros_like(img)
+            assert R.ref_conv_f32(img, w, h, m, mw, mh, b, 0, 0, r) == 0
+            out[f"conv_{mh}x{mw}_b{b}_in"] = img
+            out[f"conv_{mh}x{mw}_b{b}_mask"] = m
+            out[f"conv_{mh}x{mw}_b{b}_out"] = r
+    # Kernel::reduce over a Domain (SUM / MIN / MAX)
+    for red in (O.SUM, O.MIN, O.MAX):
+        h, w = 17, 21
+        img = rng.random((h, w), dtype=np.float32)
+        dom = (rng.random((5, 5)) > 0.35).astype(np.float32)
+        r = np.zeros_like(img)
+        R.ref_conv_f32(img, w, h, dom, 5, 5, O.MIRROR, 1, red, r)
+        out[f"domain_r{red}_in"] = img
+        out[f"domain_r{red}_dom"] = dom.astype(np.uint8)
+        out[f"domain_r{red}_out"] = r
+    # Sobel magnitude over Domains, u8, every boundary mode
+    for b in (O.CLAMP, O.REPEAT, O.MIRROR, O.CONSTANT):
+        img = rng.integers(0, 256, (21, 37), dtype=np.uint8)
+        r = np.zeros_like(img)
+        R.ref_sobel_mag_u8(img, 37, 21, O.SOBEL3_X, O.SOBEL3_Y, 3, b, r)
+        out[f"sobel_b{b}_in"] = img
+        out[f"sobel_b{b}_out"] = r
+    # RGBA -> gray
+    rgba = rng.integers(0, 256, (13, 29, 4), dtype=np.uint8)
+    g = np.zeros((13, 29), np.uint8)
+    R.ref_gray_u8(rgba, 29, 13, g)
+    out["gray_in"] = rgba
+    out["gray_out"] = g
+    # reductions
+    img = rng.integers(0, 256, (31, 45), dtype=np.uint8)
+    out["red_u8_in"] = img
+    out["red_u8_sum"] = np.array([R.ref_sum_u8_u64(img, 45, 31)], np.uint64)
+    out["red_u8_max"] = np.array([R.ref_max_u8(img, 45, 31)], np.uint32)
+    f = rng.random((29, 33), dtype=np.float32)
+    out["red_f32_in"] = f
+    out["red_f32_dsl"] = np.array([R.ref_reduce_f32(f, 33, 29, op) for op in (0, 1, 2)], np.float32)
+    out["red_f32_cpu2d_serial"] = np.array([R.ref_cpu_red_sum_f32_serial(f, 33, 29)], np.float32)
+    # bilateral (sample body with float sigma_r)
+    for size in (5, 13):
+        img = rng.random((18, 22), dtype=np.float32)
+        sm = O.spatial_mask(size, 3.0)
+        r = np.zeros_like(img)
+        R.ref_bilateral_f32(img, 22, 18, sm, size, 0.1, O.CLAMP, r)
+        out[f"bilateral_{size}_in"] = img
+        out[f"bilateral_{size}_mask"] = sm
+        out[f"bilateral_{size}_out"] = r
+    # NN / LF accessors
+    for (sw, sh, dw, dh) in [(37, 29, 18, 14), (18, 14, 37, 29)]:
+        src = rng.random((sh, sw), dtype=np.float32)
+        for mode, im in (("nn", 1), ("lf", 2)):
+            r = np.zeros((dh, dw), np.float32)
+            R.ref_resample_f32(src, sw, sh, r, dw, dh, im)
+            out[f"resample_{mode}_{sw}x{sh}_{dw}x{dh}_in"] = src
+            out[f"resample_{mode}_{sw}x{sh}_{dw}x{dh}_out"] = r
+    # Laplacian pyramid through Pyramid / traverse
+    w, h, L = 67, 45, 4
+    img = rng.random((h, w), dtype=np.float32)
+    sizes = O.level_sizes(w, h, L)
+    go = np.zeros(sum(a * b for a, b in sizes), np.float32)
+    lo = np.zeros(sum(a * b for a, b in sizes[:-1]), np.float32)
+    R.ref_pyramid_f32(img, w, h, L, O.binomial5(), O.MIRROR, go, lo)
+    out["pyramid_in"] = img
+    out["pyramid_gauss"] = go
+    out["pyramid_lap"] = lo
+    path = os.path.join(HERE, "hipacc_ref_golden.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes,", len(out), "arrays")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,77 @@
+"""CPU: the C ABI library loads, exports every declared symbol, and rejects
+bad arguments on the host before touching a device."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for fn in os.listdir(inc):
+        if fn.endswith(".h"):
+            src = open(os.path.join(inc, fn)).read()
+            names |= set(re.findall(r"HGB_API\s+[\w\s\*]*?\b(hgb_\w+)\s*\(", src))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for must in ("hgb_local_op", "hgb_sobel_mag", "hgb_point_gray", "hgb_reduce", "hgb_separable", "hgb_bilateral",
+                 "hgb_pyramid_decompose", "hgb_local_op_adjoint", "hgb_conv_bilateral_mse", "hgb_init"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(hgb_lib):
+    from hipacc_gb300 import _lib
+
+    missing = [n for n in declared_symbols() if not hasattr(hgb_lib, n)]
+    assert not missing, missing
+    # and the Python binding covers them all
+    assert declared_symbols() <= set(_lib.SIGNATURES)
+
+
+def test_abi_version(hgb_lib):
+    assert hgb_lib.hgb_abi_version() == 1
+
+
+def test_host_side_validation_without_gpu(hgb_lib):
+    """Invalid requests fail with HGB_ERR_INVALID and a message, no device call."""
+    from hipacc_gb300 import _lib as L
+
+    rc = hgb_lib.hgb_local_op(None, None, None, None, None, None, None, 3, 3, 0, 1, 0.0, None)
+    assert rc == L.ERR_INVALID
+    assert b"null view" in hgb_lib.hgb_last_error()
+    v = L.View(0x1000, L.F32, 16, 16, 1, 64, 1024)
+    bad = L.View(0x1000, L.F32, 16, 16, 1, 32, 1024)  # pitch below a row
+    rc = hgb_lib.hgb_local_op(C.byref(v), None, C.byref(bad), None, None, None, None, 3, 3, 0, 1, 0.0, None)
+    assert rc == L.ERR_INVALID and b"pitch" in hgb_lib.hgb_last_error()
+    rc = hgb_lib.hgb_local_op(C.byref(v), None, C.byref(v), None, None, None, None, 17, 3, 0, 1, 0.0, None)
+    assert rc == L.ERR_INVALID and b"mask size" in hgb_lib.hgb_last_error()
+    w = L.Window(10, 10, 10, 10)  # outside a 16x16 image
+    m = (C.c_float * 9)()
+    rc = hgb_lib.hgb_local_op(C.byref(v), C.byref(w), C.byref(v), None, m, None, None, 3, 3, 0, 1, 0.0, None)
+    assert rc == L.ERR_INVALID and b"window" in hgb_lib.hgb_last_error()
+    u8 = L.View(0x1000, L.U8, 16, 16, 1, 16, 256)
+    rc = hgb_lib.hgb_sobel_mag(C.byref(u8), C.byref(u8), None, None, 3, 3, 0, None, None, None)
+    assert rc == L.ERR_INVALID
+    rc = hgb_lib.hgb_point_gray(C.byref(u8), C.byref(u8), 77, 150, 29, 8, None)
+    assert rc == L.ERR_INVALID and b"uchar4" in hgb_lib.hgb_last_error()
+    rc = hgb_lib.hgb_reduce(C.byref(u8), None, 7, None, None, None)
+    assert rc == L.ERR_INVALID
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    from hipacc_gb300 import _lib as L
+
+    saved = L._lib
+    L._lib = None
+    try:
+        with pytest.raises(RuntimeError, match="no fallback"):
+            L.load(str(tmp_path / "nope.so"))
+    finally:
+        L._lib = saved
