@@ -55,6 +55,7 @@ SIGNATURES = {
     "hgb_autotune_save": (i32, [C.c_char_p]),
     "hgb_autotune_load": (i32, [C.c_char_p]),
     "hgb_workspace_reserve": (i32, [C.c_size_t]),
+    "hgb_device_status": (i32, [C.POINTER(C.c_int)]),
     "hgb_image_create": (i32, [i32, i32, i32, i32, vp, C.POINTER(vp)]),
     "hgb_image_destroy": (i32, [vp]),
     "hgb_image_get_view": (i32, [vp, VP]),

@@ -58,32 +58,71 @@ __device__ __forceinline__ uint32_t gray_px(const GrayParams &p, uint32_t rgba) 
   return (v >> p.shift) & 0xffu;
 }
 
-__global__ void __launch_bounds__(256) gray_kernel(const __grid_constant__ GrayParams p) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < p.rs.nitems; it += stride) {
-    const int chunk = (int)(it % p.rs.chunks_per_row);
-    const int64_t row_g = it / p.rs.chunks_per_row;
-    const int b = (int)(row_g / p.rs.rows_per_img);
-    const int row = (int)(row_g - (int64_t)b * p.rs.rows_per_img);
-    const uint8_t *src = p.in + (int64_t)b * p.in_bstride + (int64_t)row * p.in_pitch + (int64_t)chunk * 64;
-    uint8_t *dst = p.out + (int64_t)b * p.out_bstride + (int64_t)row * p.out_pitch + (int64_t)chunk * 16;
-    const int x0 = chunk * 16;
-    if (p.vec && x0 + 16 <= p.rs.row_len) {
-      uint4 a = ldg16(src), bq = ldg16(src + 16), c = ldg16(src + 32), d = ldg16(src + 48);
-      const uint32_t px[16] = {a.x, a.y, a.z, a.w, bq.x, bq.y, bq.z, bq.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
-      uint32_t o[4];
+__device__ __forceinline__ void gray_chunk_addr(const GrayParams &p, int64_t it, const uint8_t *&src, uint8_t *&dst,
+                                                int &x0) {
+  const int chunk = (int)(it % p.rs.chunks_per_row);
+  const int64_t row_g = it / p.rs.chunks_per_row;
+  const int b = (int)(row_g / p.rs.rows_per_img);
+  const int row = (int)(row_g - (int64_t)b * p.rs.rows_per_img);
+  src = p.in + (int64_t)b * p.in_bstride + (int64_t)row * p.in_pitch + (int64_t)chunk * 64;
+  dst = p.out + (int64_t)b * p.out_bstride + (int64_t)row * p.out_pitch + (int64_t)chunk * 16;
+  x0 = chunk * 16;
+}
+
+__device__ __forceinline__ uint4 gray_16(const GrayParams &p, uint4 a, uint4 bq, uint4 c, uint4 d) {
+  const uint32_t px[16] = {a.x, a.y, a.z, a.w, bq.x, bq.y, bq.z, bq.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
+  uint32_t o[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
-        o[q] = gray_px(p, px[4 * q]) | (gray_px(p, px[4 * q + 1]) << 8) | (gray_px(p, px[4 * q + 2]) << 16) |
-               (gray_px(p, px[4 * q + 3]) << 24);
-      stg16(dst, make_uint4(o[0], o[1], o[2], o[3]));
-    } else {
-      for (int q = 0; q < 16 && x0 + q < p.rs.row_len; ++q) {
-        const uint8_t *s = src + 4 * q;
-        const uint32_t rgba = (uint32_t)s[0] | ((uint32_t)s[1] << 8) | ((uint32_t)s[2] << 16) | ((uint32_t)s[3] << 24);
-        dst[q] = (uint8_t)gray_px(p, rgba);
-      }
+  for (int q = 0; q < 4; ++q)
+    o[q] = gray_px(p, px[4 * q]) | (gray_px(p, px[4 * q + 1]) << 8) | (gray_px(p, px[4 * q + 2]) << 16) |
+           (gray_px(p, px[4 * q + 3]) << 24);
+  return make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+__device__ __forceinline__ void gray_scalar(const GrayParams &p, const uint8_t *src, uint8_t *dst, int x0) {
+  for (int q = 0; q < 16 && x0 + q < p.rs.row_len; ++q) {
+    const uint8_t *s = src + 4 * q;
+    const uint32_t rgba = (uint32_t)s[0] | ((uint32_t)s[1] << 8) | ((uint32_t)s[2] << 16) | ((uint32_t)s[3] << 24);
+    dst[q] = (uint8_t)gray_px(p, rgba);
+  }
+}
+
+// Each CTA owns a contiguous range of 16-pixel chunks; a thread keeps two
+// chunks (128 bytes of loads) in flight per iteration.
+__global__ void __launch_bounds__(256) gray_kernel(const __grid_constant__ GrayParams p) {
+  const int64_t per = (p.rs.nitems + gridDim.x - 1) / gridDim.x;
+  const int64_t beg = (int64_t)blockIdx.x * per;
+  const int64_t end = beg + per < p.rs.nitems ? beg + per : p.rs.nitems;
+  for (int64_t it = beg + threadIdx.x; it < end; it += 2 * blockDim.x) {
+    const int64_t it2 = it + blockDim.x;
+    const uint8_t *s0, *s1 = nullptr;
+    uint8_t *d0, *d1 = nullptr;
+    int x0, x1 = 0;
+    gray_chunk_addr(p, it, s0, d0, x0);
+    const bool has2 = it2 < end;
+    if (has2) gray_chunk_addr(p, it2, s1, d1, x1);
+    const bool v0 = p.vec && x0 + 16 <= p.rs.row_len, v1 = has2 && p.vec && x1 + 16 <= p.rs.row_len;
+    uint4 a0, b0, c0, e0, a1, b1, c1, e1;
+    if (v0) {
+      a0 = ldg16(s0);
+      b0 = ldg16(s0 + 16);
+      c0 = ldg16(s0 + 32);
+      e0 = ldg16(s0 + 48);
     }
+    if (v1) {
+      a1 = ldg16(s1);
+      b1 = ldg16(s1 + 16);
+      c1 = ldg16(s1 + 32);
+      e1 = ldg16(s1 + 48);
+    }
+    if (v0)
+      stg16(d0, gray_16(p, a0, b0, c0, e0));
+    else
+      gray_scalar(p, s0, d0, x0);
+    if (v1)
+      stg16(d1, gray_16(p, a1, b1, c1, e1));
+    else if (has2)
+      gray_scalar(p, s1, d1, x1);
   }
 }
 
@@ -238,8 +277,15 @@ extern "C" int hgb_point_gray(const hgb_view *in, const hgb_view *out, int wr, i
   p.use_dp4a = wr < 256 && wg < 256 && wb < 256;
   p.wpack = (uint32_t)wr | ((uint32_t)wg << 8) | ((uint32_t)wb << 16);
   cudaStream_t st = (cudaStream_t)stream;
+  // one resident wave: every CTA owns one contiguous range
+  static int per_sm = 0;
+  if (!per_sm && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gray_kernel, 256, 0) != cudaSuccess)
+    per_sm = 4;
+  int grid = num_sms() * (per_sm > 0 ? per_sm : 4);
+  const int64_t need = (p.rs.nitems + 511) / 512;
+  if (need < grid) grid = (int)(need > 0 ? need : 1);
   cudaEvent_t ev = before_launch(st);
-  gray_kernel<<<grid_for(p.rs.nitems, 256), 256, 0, st>>>(p);
+  gray_kernel<<<grid, 256, 0, st>>>(p);
   return after_launch("gray_kernel", st, ev);
 }
 

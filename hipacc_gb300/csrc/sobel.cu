@@ -7,15 +7,17 @@
 // Kernel::reduced_data of the output with a u64 sum and a u8 max
 // (dsl/kernel.hpp:121-161).  Integer arithmetic, so every order is exact.
 //
-// Fast path (the standard 3x3 Sobel masks): a CTA stages a 128 x 64 output
-// tile plus a one-pixel halo as bytes in shared memory (16-byte loads, remap
-// only on border tiles).  A thread owns 4 adjacent columns x 8 rows, walks the
+// Fast path (the standard 3x3 Sobel masks, TMA-legal layout): sobel3_tma_kernel
+// below -- persistent CTAs, TMA double-buffered halo tiles, exact fp16x2
+// arithmetic.  Fallback for layouts TMA cannot address (unaligned base or
+// pitch): sobel3_kernel, which stages a 128 x 64 tile with 16-byte loads, walks
 // rows with a three-row register window and uses the separable form
 // gx = S(x+1) - S(x-1), S = top + 2 mid + bottom; gy = D(x-1) + 2 D(x) + D(x+1),
-// D = bottom - top.  The result is written as one 32-bit word per row; sum and
-// max are reduced with redux.sync across the warp, shared memory across the
-// block and a last-block combine of the per-block partials.
+// D = bottom - top.  Other masks: sobel_generic_kernel.  Every path reduces
+// sum and max with redux.sync across the warp, shared memory across the block
+// and a last-block combine of the per-block partials.
 #include "reduce_common.cuh"
+#include "tma.cuh"
 
 namespace hgb {
 
@@ -202,6 +204,210 @@ __global__ void __launch_bounds__(SB_BX *SB_BY) sobel3_kernel(const __grid_const
   if (p.sum_dev || p.max_dev) block_reduce_store(p, tsum, tmax);
 }
 
+
+// ---------------------------------------------------------------------------
+// TMA path for the standard 3x3 masks.  Persistent CTAs each own a contiguous
+// range of 128 x 32 output tiles (about SMs x 8 CTAs, equal tile counts).  The
+// 160 x 34 byte halo tile of each is loaded by cp.async.bulk.tensor into a
+// 4-stage ring, so a CTA has up to four tiles in flight from its first cycle.
+// Cells outside the image (TMA fills them with 0) are patched with the
+// boundary rule before use.  Arithmetic is fp16x2 on exact integers: every
+// intermediate (|gx|, |gy| <= 1020, their sum <= 2040) is an integer below
+// 2048 and therefore exact in half precision, so results are the integer
+// results bit for bit.  Bytes become halves by placing them under the
+// exponent byte 0x64 (1024 + v) with one byte permute per pair.
+struct SobelTmaParams {
+  CUtensorMap map;
+  SobelParams p;
+  int tiles_x, tiles_y, ntiles, tiles_per_cta;
+  int *status;
+};
+
+constexpr int T_TW = 128, T_TH = 32, T_BX = 32, T_BY = 4, T_PY = 8;
+constexpr int T_SW = 160, T_SH = T_TH + 2, T_STAGE = T_SW * T_SH;
+constexpr int T_STAGE_PAD = (T_STAGE + 127) / 128 * 128;
+constexpr int T_NST = 4;
+
+__device__ __forceinline__ __half2 u2h(uint32_t u) {
+  __half2 h;
+  memcpy(&h, &u, 4);
+  return h;
+}
+__device__ __forceinline__ uint32_t h2u(__half2 h) {
+  uint32_t u;
+  memcpy(&u, &h, 4);
+  return u;
+}
+
+// One staged tile through the stencil.  FULL: every output of the tile is
+// inside the image and 4-byte stores are legal (no masks, no edge branches).
+template <bool FULL>
+__device__ __forceinline__ void sobel_tile(const SobelParams &p, const uint8_t *tile, uint8_t *out_row, int xo, int yo,
+                                           int xs, int r0, uint32_t &tsum, __half2 &tmax) {
+  const uint32_t K = 0x64646464u;
+  const __half2 c1024 = __float2half2_rn(1024.0f), c255 = __float2half2_rn(255.0f), two = __float2half2_rn(2.0f);
+  __half2 H01[T_PY + 2], H23[T_PY + 2], R01[T_PY + 2], R23[T_PY + 2];
+#pragma unroll
+  for (int r = 0; r < T_PY + 2; ++r) {
+    const uint8_t *row = tile + (r0 + r) * T_SW + xs;
+    const uint32_t w0 = *reinterpret_cast<const uint32_t *>(row - 4);
+    const uint32_t w1 = *reinterpret_cast<const uint32_t *>(row);
+    const uint32_t w2 = *reinterpret_cast<const uint32_t *>(row + 4);
+    const uint32_t f1 = __funnelshift_r(w0, w1, 24);  // x-1 .. x+2
+    const uint32_t f2 = __funnelshift_r(w1, w2, 24);  // x+3 .. x+6
+    const __half2 Pa = __hsub2(u2h(__byte_perm(f1, K, 0x4140)), c1024);  // (x-1, x)
+    const __half2 Pb = __hsub2(u2h(__byte_perm(w1, K, 0x4140)), c1024);  // (x, x+1)
+    const __half2 Pc = __hsub2(u2h(__byte_perm(f1, K, 0x4342)), c1024);  // (x+1, x+2)
+    const __half2 Pd = __hsub2(u2h(__byte_perm(w1, K, 0x4342)), c1024);  // (x+2, x+3)
+    const __half2 Pe = __hsub2(u2h(__byte_perm(f2, K, 0x4140)), c1024);  // (x+3, x+4)
+    H01[r] = __hsub2(Pc, Pa);
+    H23[r] = __hsub2(Pe, Pc);
+    R01[r] = __hfma2(two, Pb, __hadd2(Pa, Pc));
+    R23[r] = __hfma2(two, Pd, __hadd2(Pc, Pe));
+  }
+  __half2 v01, v23;
+  if constexpr (!FULL) {
+    v01 = __halves2half2(__float2half(xo < p.w ? 1.f : 0.f), __float2half(xo + 1 < p.w ? 1.f : 0.f));
+    v23 = __halves2half2(__float2half(xo + 2 < p.w ? 1.f : 0.f), __float2half(xo + 3 < p.w ? 1.f : 0.f));
+  }
+#pragma unroll
+  for (int o = 0; o < T_PY; ++o) {
+    const __half2 gx01 = __hfma2(two, H01[o + 1], __hadd2(H01[o], H01[o + 2]));
+    const __half2 gx23 = __hfma2(two, H23[o + 1], __hadd2(H23[o], H23[o + 2]));
+    const __half2 gy01 = __hsub2(R01[o + 2], R01[o]);
+    const __half2 gy23 = __hsub2(R23[o + 2], R23[o]);
+    __half2 m01 = __hmin2(__hadd2(__habs2(gx01), __habs2(gy01)), c255);
+    __half2 m23 = __hmin2(__hadd2(__habs2(gx23), __habs2(gy23)), c255);
+    bool row_ok = true;
+    if constexpr (!FULL) {
+      row_ok = yo + o < p.h;
+      m01 = row_ok ? __hmul2(m01, v01) : __float2half2_rn(0.0f);
+      m23 = row_ok ? __hmul2(m23, v23) : __float2half2_rn(0.0f);
+    }
+    const uint32_t word = __byte_perm(h2u(__hadd2(m01, c1024)), h2u(__hadd2(m23, c1024)), 0x6420);
+    tsum = __dp4a(word, 0x01010101u, tsum);
+    tmax = __hmax2(tmax, __hmax2(m01, m23));
+    uint8_t *dst = out_row + (int64_t)o * p.out_pitch;
+    if constexpr (FULL) {
+      *reinterpret_cast<uint32_t *>(dst) = word;
+    } else if (row_ok) {
+      if (p.vec_out && xo + 4 <= p.w) {
+        *reinterpret_cast<uint32_t *>(dst) = word;
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (xo + q < p.w) dst[q] = (uint8_t)(word >> (8 * q));
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(T_BX *T_BY, 8) sobel3_tma_kernel(const __grid_constant__ SobelTmaParams P) {
+  __shared__ __align__(128) uint8_t buf[T_NST * T_STAGE_PAD];
+  __shared__ __align__(8) uint64_t bar[T_NST];
+  __shared__ int s_coord[3];
+  const SobelParams &p = P.p;
+  const int tid = threadIdx.x;
+  const int t0 = blockIdx.x * P.tiles_per_cta;
+  const int nt = min(P.tiles_per_cta, P.ntiles - t0);
+  auto coords = [&](int t, int &b, int &i0, int &j0) {
+    const int tx_ = t % P.tiles_x;
+    const int r = t / P.tiles_x;
+    j0 = (r % P.tiles_y) * T_TH;
+    b = r / P.tiles_y;
+    i0 = tx_ * T_TW;
+  };
+  auto issue = [&](int k) {
+    int b, i0, j0;
+    coords(t0 + k, b, i0, j0);
+    const int st = k % T_NST;
+    fence_proxy_async_smem();
+    mbar_expect_tx(&bar[st], T_STAGE);
+    tma_load_3d(buf + st * T_STAGE_PAD, &P.map, i0 - 16, j0 - 1, b, &bar[st]);
+  };
+  if (tid == 0) {
+    for (int i = 0; i < T_NST; ++i) mbar_init(&bar[i], 1);
+    mbar_fence_init();
+    for (int k = 0; k < T_NST && k < nt; ++k) issue(k);
+  }
+  __syncthreads();
+
+  const int tx = tid % T_BX, ty = tid / T_BX;
+  const int xs = 16 + 4 * tx, r0 = T_PY * ty;
+  uint32_t tsum = 0;
+  __half2 tmax = __float2half2_rn(0.0f);
+  for (int k = 0; k < nt; ++k) {
+    const int st = k % T_NST;
+    // one thread polls the mbarrier; the others block in the hardware barrier
+    // (its CTA-scope ordering publishes the TMA bytes the poller acquired)
+    int ok = 1;
+    if (tid == 0) {
+      ok = mbar_wait(&bar[st], (k / T_NST) & 1);
+      int b, i0, j0;
+      coords(t0 + k, b, i0, j0);
+      s_coord[0] = b;
+      s_coord[1] = i0;
+      s_coord[2] = j0;
+    }
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        record_status(P.status, HGB_ERR_TIMEOUT);
+        for (int j = k + 1; j < nt && j < k + T_NST; ++j) mbar_wait(&bar[j % T_NST], (j / T_NST) & 1);
+      }
+      break;
+    }
+    const int b = s_coord[0], i0 = s_coord[1], j0 = s_coord[2];
+    uint8_t *tile = buf + st * T_STAGE_PAD;
+    const int X0 = i0 - 16, Y0 = j0 - 1;
+    if (X0 + 15 < 0 || X0 + 145 > p.w || Y0 < 0 || Y0 + T_SH > p.h) {
+      // Patch the staged cells outside the image that the stencil reads
+      // (columns 15..144, all rows) with the boundary rule; TMA filled them
+      // with zeros.  Regions: left columns, right columns, top row, bottom rows.
+      const uint8_t *img = p.in + (int64_t)b * p.in_bstride;
+      constexpr int qa = 15, qb = 145, ncol = qb - qa;
+      const int nl = max(0, min(qb, -X0) - qa);
+      const int rs = max(qa, p.w - X0), nr = max(0, qb - rs);
+      const int ntop = max(0, -Y0);
+      const int bs = max(0, p.h - Y0), nb = max(0, T_SH - bs);
+      const int n1 = nl * T_SH, n2 = n1 + nr * T_SH, n3 = n2 + ntop * ncol, n4 = n3 + nb * ncol;
+      for (int c = tid; c < n4; c += T_BX * T_BY) {
+        int r, q;
+        if (c < n1) {
+          r = c / nl;
+          q = qa + (c - r * nl);
+        } else if (c < n2) {
+          const int d = c - n1;
+          r = d / nr;
+          q = rs + (d - r * nr);
+        } else if (c < n3) {
+          const int d = c - n2;
+          r = d / ncol;
+          q = qa + (d - r * ncol);
+        } else {
+          const int d = c - n3;
+          const int rr = d / ncol;
+          r = bs + rr;
+          q = qa + (d - rr * ncol);
+        }
+        tile[r * T_SW + q] = (uint8_t)sb_load_px(p, img, X0 + q, Y0 + r);
+      }
+      __syncthreads();
+    }
+    const int xo = i0 + 4 * tx, yo = j0 + r0;
+    uint8_t *out_row = p.out + (int64_t)b * p.out_bstride + (int64_t)yo * p.out_pitch + xo;
+    if (p.vec_out && i0 + T_TW <= p.w && j0 + T_TH <= p.h)
+      sobel_tile<true>(p, tile, out_row, xo, yo, xs, r0, tsum, tmax);
+    else
+      sobel_tile<false>(p, tile, out_row, xo, yo, xs, r0, tsum, tmax);
+    __syncthreads();  // the stage is read; refill it with the tile T_NST ahead
+    if (tid == 0 && k + T_NST < nt) issue(k + T_NST);
+  }
+  if (p.sum_dev || p.max_dev) {
+    const float2 mf = __half22float2(tmax);
+    block_reduce_store(p, tsum, (uint32_t)fmaxf(mf.x, mf.y));
+  }
+}
+
 // Any integer masks of size 3, 5 or 7: one pixel per thread, runtime
 // coefficients, zero cells skipped (Domain semantics).
 __global__ void __launch_bounds__(256) sobel_generic_kernel(const __grid_constant__ SobelParams p) {
@@ -291,6 +497,38 @@ extern "C" int hgb_sobel_mag(const hgb_view *in, const hgb_view *out, const int 
     p.ticket = ws.tickets + 0;
   }
   cudaStream_t st = (cudaStream_t)stream;
+  if (fast && tma_legal(in->data, in->pitch, in->batch_stride, in->batch)) {
+    SobelTmaParams P;
+    memset(&P, 0, sizeof(P));
+    P.p = p;
+    P.tiles_x = cdiv(p.w, T_TW);
+    P.tiles_y = cdiv(p.h, T_TH);
+    P.ntiles = P.tiles_x * P.tiles_y * in->batch;
+    P.status = device_status_word();
+    rc = make_tensor_map_3d(&P.map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, in->data, p.w, p.h, in->batch, in->pitch,
+                            in->batch_stride, T_SW, T_SH);
+    if (rc == HGB_OK) {
+      // equal contiguous tile ranges over about one resident wave of CTAs
+      static int per_sm = 0;
+      if (!per_sm &&
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sobel3_tma_kernel, T_BX * T_BY, 0) != cudaSuccess)
+        per_sm = 4;
+      const int max_ctas = num_sms() * (per_sm > 0 ? per_sm : 4);
+      P.tiles_per_cta = cdiv(P.ntiles, max_ctas);
+      const int g = cdiv(P.ntiles, P.tiles_per_cta);
+      if (sum_dev || max_dev) {
+        Workspace ws;
+        rc = workspace_get((size_t)g * 12 + 256, &ws);
+        if (rc) return rc;
+        P.p.partials = (uint2 *)ws.base;
+        P.p.partial_max = (uint32_t *)((char *)ws.base + (size_t)g * 8);
+        P.p.ticket = ws.tickets + 0;
+      }
+      cudaEvent_t ev = before_launch(st);
+      sobel3_tma_kernel<<<g, T_BX * T_BY, 0, st>>>(P);
+      return after_launch("sobel3_tma_kernel", st, ev);
+    }
+  }
   cudaEvent_t ev = before_launch(st);
   if (fast)
     sobel3_kernel<<<grid, SB_BX * SB_BY, 0, st>>>(p);

@@ -122,6 +122,11 @@ HGB_API int hgb_autotune_count(void);
 HGB_API int hgb_autotune_save(const char *path);
 HGB_API int hgb_autotune_load(const char *path);
 
+/* Device status word: HGB_OK, or the error a kernel recorded since the last
+ * call (HGB_ERR_TIMEOUT when a bounded wait on a TMA copy or an inter-tile
+ * dependency expired).  Synchronises the device and clears the word. */
+HGB_API int hgb_device_status(int *status);
+
 /* Reserve the per-device workspace (reduction partials, tickets, work-lists)
  * up front, e.g. before stream capture.  Calls grow it on demand otherwise. */
 HGB_API int hgb_workspace_reserve(size_t bytes);
