@@ -41,8 +41,13 @@ struct Workspace {
   void *base = nullptr;     // general scratch
   size_t bytes = 0;
   unsigned int *tickets = nullptr;  // kTickets counters, zero between uses
+  unsigned long long *acc = nullptr;  // kAcc accumulators, zero between uses
 };
 constexpr int kTickets = 64;
+constexpr int kAcc = 64;
+// accumulator / ticket slots of the fused and standalone reductions
+constexpr int kSlotSobel = 0;   // acc[0] sum, acc[1] max; ticket[0]
+constexpr int kSlotReduce = 2;  // acc[2]; ticket[1]
 int workspace_get(size_t bytes, Workspace *ws);  // grows on demand
 
 int num_sms();

@@ -118,6 +118,7 @@ struct RedParams {
   int vec;
   void *partials;
   unsigned int *ticket;
+  unsigned long long *acc;  // integer accumulator (zero at rest)
   unsigned long long *result_dev;
 };
 
@@ -175,6 +176,35 @@ __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ Red
     }
   }
   acc = block_fold<T, OP>(acc);
+  if constexpr (std::is_integral<T>::value && OP != HGB_REDUCE_PROD) {
+    // integers: order-preserving 64-bit keys folded with relaxed atomics,
+    // published by the CTA that takes the last ticket (no combine loop)
+    using R2 = Red<T, OP>;
+    constexpr unsigned long long kSign = R2::kSigned ? 0x8000000000000000ull : 0ull;
+    if (threadIdx.x == 0) {
+      const unsigned long long u = (unsigned long long)acc ^ kSign;
+      if (OP == HGB_REDUCE_SUM)
+        atomicAdd(p.acc, (unsigned long long)acc);
+      else if (OP == HGB_REDUCE_MAX)
+        atomicMax(p.acc, u);
+      else
+        atomicMax(p.acc, ~u);
+      if (ticket_acq_rel(p.ticket) == gridDim.x - 1) {
+        const unsigned long long v = ld_relaxed_u64(p.acc);
+        A a;
+        if (OP == HGB_REDUCE_SUM)
+          a = (A)v;
+        else if (OP == HGB_REDUCE_MAX)
+          a = (A)(v ^ kSign);
+        else
+          a = (A)(~v ^ kSign);
+        *p.result_dev = R2::finish(a);
+        *p.acc = 0ull;
+        *p.ticket = 0u;
+      }
+    }
+    return;
+  }
   A *parts = reinterpret_cast<A *>(p.partials);
   if (threadIdx.x == 0) parts[blockIdx.x] = acc;
   if (!take_last_ticket(p.ticket)) return;
@@ -274,6 +304,7 @@ extern "C" int hgb_reduce(const hgb_view *in, const hgb_window *winp, int op, vo
   unsigned long long *slot = (unsigned long long *)((char *)ws.base + ((size_t)grid * 16 + 15) / 16 * 16);
   p.result_dev = result_dev ? (unsigned long long *)result_dev : slot;
   p.ticket = ws.tickets + 1;
+  p.acc = ws.acc + kSlotReduce;
   cudaStream_t st = (cudaStream_t)stream;
   switch (in->dtype) {
     case HGB_U8: rc = launch_reduce<uint8_t>(op, p, grid, st); break;

@@ -20,21 +20,56 @@ __device__ __forceinline__ unsigned int block_rank() {
 
 // Call after thread 0 stored this block's partial.  Returns true (in all
 // threads of the block) in the block that must combine.
+__device__ __forceinline__ unsigned int ticket_acq_rel(unsigned int *t);
 __device__ __forceinline__ bool take_last_ticket(unsigned int *ticket) {
   __shared__ bool s_last;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned int t = atomicAdd(ticket, 1u);
-    s_last = (t == grid_blocks() - 1);
-  }
+  // thread 0 stored the block's partial; its acq_rel ticket releases it, and
+  // in the last block acquires every other block's partial.  The barrier then
+  // orders the other threads' reads of the partials after that acquire.
+  if (threadIdx.x == 0) s_last = (ticket_acq_rel(ticket) == grid_blocks() - 1);
   __syncthreads();
-  if (s_last) __threadfence();
   return s_last;
 }
 
 __device__ __forceinline__ void release_ticket(unsigned int *ticket) {
   if (threadIdx.x == 0) *ticket = 0u;
+}
+
+// Ticket increment with acquire-release semantics at GPU scope: it releases
+// this thread's earlier (relaxed) accumulator atomics and, in the last CTA,
+// acquires everyone's.
+__device__ __forceinline__ unsigned int ticket_acq_rel(unsigned int *t) {
+  unsigned int old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(t) : "memory");
+  return old;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Single-pass integer reduction epilogue without a combine loop: thread 0 of
+// every CTA folds its block value into the accumulators with relaxed atomics
+// (no return value, so they issue as reductions) and takes the ticket; the CTA
+// that takes the last ticket copies the accumulators out and zeroes them and
+// the ticket for the next launch.  Only one atomic round trip per CTA.
+__device__ __forceinline__ void accumulate_and_publish(unsigned long long *acc_sum, unsigned long long *acc_max,
+                                                       unsigned int *ticket, unsigned long long bsum,
+                                                       unsigned long long bmax, uint64_t *sum_dev,
+                                                       uint32_t *max_dev) {
+  if (threadIdx.x != 0) return;
+  if (bsum) atomicAdd(acc_sum, bsum);
+  if (bmax) atomicMax(acc_max, bmax);
+  if (ticket_acq_rel(ticket) == grid_blocks() - 1) {
+    const unsigned long long s = ld_relaxed_u64(acc_sum), m = ld_relaxed_u64(acc_max);
+    if (sum_dev) *sum_dev = s;
+    if (max_dev) *max_dev = (uint32_t)m;
+    *acc_sum = 0ull;
+    *acc_max = 0ull;
+    *ticket = 0u;
+  }
 }
 
 template <typename T>

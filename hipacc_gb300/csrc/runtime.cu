@@ -78,11 +78,14 @@ int workspace_get(size_t bytes, Workspace *ws) {
   std::lock_guard<std::mutex> lk(g_mu);
   DeviceState &st = dev_state(dev);
   if (!st.ws.tickets) {
+    // accumulators first (8-byte aligned), tickets behind them
     void *t = nullptr;
-    HGB_CHECK_CUDA(cudaMalloc(&t, kTickets * sizeof(unsigned int)));
-    HGB_CHECK_CUDA(cudaMemset(t, 0, kTickets * sizeof(unsigned int)));
+    const size_t nb = kAcc * sizeof(unsigned long long) + kTickets * sizeof(unsigned int);
+    HGB_CHECK_CUDA(cudaMalloc(&t, nb));
+    HGB_CHECK_CUDA(cudaMemset(t, 0, nb));
     HGB_CHECK_CUDA(cudaDeviceSynchronize());
-    st.ws.tickets = (unsigned int *)t;
+    st.ws.acc = (unsigned long long *)t;
+    st.ws.tickets = (unsigned int *)((char *)t + kAcc * sizeof(unsigned long long));
   }
   if (st.ws.bytes < bytes) {
     // Growing replaces the buffer: wait for every stream of the device that

@@ -221,6 +221,8 @@ struct SobelTmaParams {
   SobelParams p;
   int tiles_x, tiles_y, ntiles, tiles_per_cta;
   int *status;
+  unsigned long long *acc;  // workspace accumulators (sum, max), zero at rest
+  unsigned int *ticket;
 };
 
 constexpr int T_TW = 128, T_TH = 32, T_BX = 32, T_BY = 4, T_PY = 8;
@@ -241,41 +243,46 @@ __device__ __forceinline__ uint32_t h2u(__half2 h) {
 
 // One staged tile through the stencil.  FULL: every output of the tile is
 // inside the image and 4-byte stores are legal (no masks, no edge branches).
+// Rows stream through a three-row window of biased pairs P = 1024 + v:
+// row differences H = P(x+1) - P(x-1) and vertical differences
+// V = P(bottom) - P(top) cancel the bias exactly, so
+// gx = H_top + 2 H_mid + H_bottom and gy = V(x-1) + 2 V(x) + V(x+1).
 template <bool FULL>
 __device__ __forceinline__ void sobel_tile(const SobelParams &p, const uint8_t *tile, uint8_t *out_row, int xo, int yo,
                                            int xs, int r0, uint32_t &tsum, __half2 &tmax) {
   const uint32_t K = 0x64646464u;
   const __half2 c1024 = __float2half2_rn(1024.0f), c255 = __float2half2_rn(255.0f), two = __float2half2_rn(2.0f);
-  __half2 H01[T_PY + 2], H23[T_PY + 2], R01[T_PY + 2], R23[T_PY + 2];
-#pragma unroll
-  for (int r = 0; r < T_PY + 2; ++r) {
-    const uint8_t *row = tile + (r0 + r) * T_SW + xs;
-    const uint32_t w0 = *reinterpret_cast<const uint32_t *>(row - 4);
-    const uint32_t w1 = *reinterpret_cast<const uint32_t *>(row);
-    const uint32_t w2 = *reinterpret_cast<const uint32_t *>(row + 4);
-    const uint32_t f1 = __funnelshift_r(w0, w1, 24);  // x-1 .. x+2
-    const uint32_t f2 = __funnelshift_r(w1, w2, 24);  // x+3 .. x+6
-    const __half2 Pa = __hsub2(u2h(__byte_perm(f1, K, 0x4140)), c1024);  // (x-1, x)
-    const __half2 Pb = __hsub2(u2h(__byte_perm(w1, K, 0x4140)), c1024);  // (x, x+1)
-    const __half2 Pc = __hsub2(u2h(__byte_perm(f1, K, 0x4342)), c1024);  // (x+1, x+2)
-    const __half2 Pd = __hsub2(u2h(__byte_perm(w1, K, 0x4342)), c1024);  // (x+2, x+3)
-    const __half2 Pe = __hsub2(u2h(__byte_perm(f2, K, 0x4140)), c1024);  // (x+3, x+4)
-    H01[r] = __hsub2(Pc, Pa);
-    H23[r] = __hsub2(Pe, Pc);
-    R01[r] = __hfma2(two, Pb, __hadd2(Pa, Pc));
-    R23[r] = __hfma2(two, Pd, __hadd2(Pc, Pe));
-  }
+  __half2 P[3][5], H01[3], H23[3];
   __half2 v01, v23;
   if constexpr (!FULL) {
     v01 = __halves2half2(__float2half(xo < p.w ? 1.f : 0.f), __float2half(xo + 1 < p.w ? 1.f : 0.f));
     v23 = __halves2half2(__float2half(xo + 2 < p.w ? 1.f : 0.f), __float2half(xo + 3 < p.w ? 1.f : 0.f));
   }
 #pragma unroll
-  for (int o = 0; o < T_PY; ++o) {
-    const __half2 gx01 = __hfma2(two, H01[o + 1], __hadd2(H01[o], H01[o + 2]));
-    const __half2 gx23 = __hfma2(two, H23[o + 1], __hadd2(H23[o], H23[o + 2]));
-    const __half2 gy01 = __hsub2(R01[o + 2], R01[o]);
-    const __half2 gy23 = __hsub2(R23[o + 2], R23[o]);
+  for (int r = 0; r < T_PY + 2; ++r) {
+    const int c = r % 3;
+    const uint8_t *row = tile + (r0 + r) * T_SW + xs;
+    const uint32_t w0 = *reinterpret_cast<const uint32_t *>(row - 4);
+    const uint32_t w1 = *reinterpret_cast<const uint32_t *>(row);
+    const uint32_t w2 = *reinterpret_cast<const uint32_t *>(row + 4);
+    const uint32_t f1 = __funnelshift_r(w0, w1, 24);  // x-1 .. x+2
+    const uint32_t f2 = __funnelshift_r(w1, w2, 24);  // x+3 .. x+6
+    P[c][0] = u2h(__byte_perm(f1, K, 0x4140));  // (x-1, x)
+    P[c][1] = u2h(__byte_perm(w1, K, 0x4140));  // (x, x+1)
+    P[c][2] = u2h(__byte_perm(f1, K, 0x4342));  // (x+1, x+2)
+    P[c][3] = u2h(__byte_perm(w1, K, 0x4342));  // (x+2, x+3)
+    P[c][4] = u2h(__byte_perm(f2, K, 0x4140));  // (x+3, x+4)
+    H01[c] = __hsub2(P[c][2], P[c][0]);
+    H23[c] = __hsub2(P[c][4], P[c][2]);
+    if (r < 2) continue;
+    const int o = r - 2, ct = (r - 2) % 3, cm = (r - 1) % 3;  // top, middle; c is the bottom row
+    const __half2 gx01 = __hfma2(two, H01[cm], __hadd2(H01[ct], H01[c]));
+    const __half2 gx23 = __hfma2(two, H23[cm], __hadd2(H23[ct], H23[c]));
+    __half2 V[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) V[q] = __hsub2(P[c][q], P[ct][q]);
+    const __half2 gy01 = __hfma2(two, V[1], __hadd2(V[0], V[2]));
+    const __half2 gy23 = __hfma2(two, V[3], __hadd2(V[2], V[4]));
     __half2 m01 = __hmin2(__hadd2(__habs2(gx01), __habs2(gy01)), c255);
     __half2 m23 = __hmin2(__hadd2(__habs2(gx23), __habs2(gy23)), c255);
     bool row_ok = true;
@@ -404,7 +411,23 @@ __global__ void __launch_bounds__(T_BX *T_BY, 8) sobel3_tma_kernel(const __grid_
   }
   if (p.sum_dev || p.max_dev) {
     const float2 mf = __half22float2(tmax);
-    block_reduce_store(p, tsum, (uint32_t)fmaxf(mf.x, mf.y));
+    uint32_t bs = __reduce_add_sync(0xffffffffu, tsum);
+    uint32_t bm = __reduce_max_sync(0xffffffffu, (uint32_t)fmaxf(mf.x, mf.y));
+    __shared__ uint32_t s_sum[T_BX * T_BY / 32], s_max[T_BX * T_BY / 32];
+    if ((tid & 31) == 0) {
+      s_sum[tid >> 5] = bs;
+      s_max[tid >> 5] = bm;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      unsigned long long S = 0, M = 0;
+#pragma unroll
+      for (int i = 0; i < T_BX * T_BY / 32; ++i) {
+        S += s_sum[i];
+        M = M > s_max[i] ? M : s_max[i];
+      }
+      accumulate_and_publish(P.acc, P.acc + 1, P.ticket, S, M, p.sum_dev, p.max_dev);
+    }
   }
 }
 
@@ -518,11 +541,10 @@ extern "C" int hgb_sobel_mag(const hgb_view *in, const hgb_view *out, const int 
       const int g = cdiv(P.ntiles, P.tiles_per_cta);
       if (sum_dev || max_dev) {
         Workspace ws;
-        rc = workspace_get((size_t)g * 12 + 256, &ws);
+        rc = workspace_get(0, &ws);
         if (rc) return rc;
-        P.p.partials = (uint2 *)ws.base;
-        P.p.partial_max = (uint32_t *)((char *)ws.base + (size_t)g * 8);
-        P.p.ticket = ws.tickets + 0;
+        P.acc = ws.acc + kSlotSobel;
+        P.ticket = ws.tickets + 0;
       }
       cudaEvent_t ev = before_launch(st);
       sobel3_tma_kernel<<<g, T_BX * T_BY, 0, st>>>(P);
