@@ -72,6 +72,7 @@ SIGNATURES = {
     "hgb_convert": (i32, [VP, VP, vp]),
     "hgb_resample": (i32, [VP, VP, i32, vp]),
     "hgb_reduce": (i32, [VP, WP, i32, vp, vp, vp]),
+    "hgb_reduce_noalloc": (i32, [VP, WP, i32, vp, vp, vp]),
     "hgb_pyramid_plan_create": (i32, [i32, vp, vp, i32, vp, i32, C.POINTER(vp)]),
     "hgb_pyramid_plan_destroy": (i32, [vp]),
     "hgb_pyramid_level_view": (i32, [vp, i32, i32, VP, VP]),

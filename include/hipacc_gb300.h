@@ -228,6 +228,20 @@ HGB_API int hgb_resample(const hgb_view *in, const hgb_view *out, int imode, voi
 HGB_API int hgb_reduce(const hgb_view *in, const hgb_window *win, int op, void *result_dev, void *result_host,
                void *stream);
 
+/* hgb_reduce for callers that cannot allocate device memory (no counterpart
+ * in the reference).  hgb_reduce grows a library workspace with cudaMalloc on
+ * first use; code that runs during stream capture, real-time loops that must
+ * not block in the allocator, or hosts whose device memory belongs to another
+ * allocator cannot allow that.  This entry point allocates nothing: its
+ * scratch is a fixed 16.25 KiB array in the library's device memory (block
+ * partials for at most 1024 blocks; larger launches return HGB_ERR_LIMIT),
+ * held by every GPU that loads the library until exit.  The first call on a
+ * device resolves the array's address (make it before any stream capture).
+ * Every call shares the array: calls that overlap on the GPU race.  Same
+ * arguments, results and determinism as hgb_reduce. */
+HGB_API int hgb_reduce_noalloc(const hgb_view *in, const hgb_window *win, int op, void *result_dev,
+                               void *result_host, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* pyramids (Pyramid / traverse, dsl/pyramid.hpp:97-318;                */
 /* hipaccCreatePyramid, runtime/hipacc_cu.tpp:466-497)                  */
