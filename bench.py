@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-extras", action="store_true", help="skip the other workloads' kernel timings")
     return ap.parse_args()
 
 
@@ -311,6 +312,7 @@ def run_gb300(args):
     except (OSError, ValueError):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
+    others = measure_other_configs(dev, peak) if (rank == 0 and not args.no_extras) else None
     dom = kern["gray_kernel"]
     if rank == 0:
         line = {
@@ -327,6 +329,7 @@ def run_gb300(args):
                          "frac": dom["achieved_gbs"] / peak, "traffic": None, "kernel": "gray_kernel",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},
             "kernels": kern,
+            "other_configs": others,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_px / e2e_max / 1e9, "unit": "Gpixels/s", "h2d_bytes_per_step": e2e["h2d"],
                     "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"]},
@@ -336,6 +339,100 @@ def run_gb300(args):
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+def graph_time_us(fn, n, stream, reps):
+    """Average device time of fn(i) (i = 0..n-1, one launch each) replayed from
+    a CUDA graph on `stream`, in microseconds per launch."""
+    import torch
+
+    with torch.cuda.stream(stream):
+        for i in range(n):
+            fn(i)
+    torch.cuda.synchronize()
+    gr = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gr, stream=stream):
+        for i in range(n):
+            fn(i)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        gr.replay()
+        a.record(stream)
+        for _ in range(reps):
+            gr.replay()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) * 1e3 / (reps * n)
+
+
+def field(h, w, seed, dev):
+    """Smooth 2-D sinusoid plus N(0, 0.05) noise clipped to [0, 1] (the
+    precision workload's image), generated on the device."""
+    import torch
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    y = torch.arange(h, device=dev, dtype=torch.float32)[:, None]
+    x = torch.arange(w, device=dev, dtype=torch.float32)[None, :]
+    f = 0.5 + 0.25 * torch.sin(2 * np.pi * x / 512.0) * torch.cos(2 * np.pi * y / 384.0)
+    f = f + 0.05 * torch.randn((h, w), device=dev, generator=g)
+    return f.clamp_(0.0, 1.0)
+
+
+def gauss_taps(k, sigma):
+    ax = np.arange(-(k // 2), k // 2 + 1, dtype=np.float64)
+    g = np.exp(-ax ** 2 / (2 * sigma * sigma))
+    return (g / g.sum()).astype(np.float32)
+
+
+def measure_other_configs(dev, peak_gbs):
+    """Device throughput of the other workloads (graph-replayed, inputs larger than L2)."""
+    import torch
+
+    from hipacc_gb300 import api
+
+    s = torch.cuda.Stream(device=dev)
+    res = {}
+    # 5x5 sigma=1 Gaussian, FP32 1024x1024, CLAMP: batches of 64 distinct images per launch
+    ax = np.arange(-2, 3, dtype=np.float64)
+    m5 = np.exp(-(ax[None, :] ** 2 + ax[:, None] ** 2) / 2.0)
+    m5 = (m5 / m5.sum()).astype(np.float32)
+    nb = 4
+    ins = [torch.rand((64, 1024, 1024), device=dev) for _ in range(nb)]
+    outs = [torch.empty_like(x) for x in ins]
+    us = graph_time_us(lambda i: api.local_op(ins[i % nb], outs[i % nb], mask=m5, boundary=api.CLAMP, stream=s), nb,
+                       s, 10)
+    px = 64 * 1024 * 1024
+    res["gaussian5x5_f32_1024_clamp_b64"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                             "achieved_gbs": 8 * px / us / 1e3, "frac_hbm": 8 * px / us / 1e3 / peak_gbs}
+    del ins, outs
+    # precision: separable 9x9 sigma=2 and 13x13 bilateral on 8192x8192, REPEAT
+    img32 = [field(8192, 8192, 20 + i, dev) for i in range(2)]
+    taps = gauss_taps(9, 2.0)
+    ax = np.arange(-6, 7, dtype=np.float64)
+    sm = np.exp(-(ax[None, :] ** 2 + ax[:, None] ** 2) / (2 * 9.0)).astype(np.float32)
+    px = 8192 * 8192
+    for name, dt in (("f32", torch.float32), ("bf16", torch.bfloat16), ("f16", torch.float16)):
+        ins = [x.to(dt) for x in img32]
+        outs = [torch.empty_like(x) for x in ins]
+        es = ins[0].element_size()
+        us = graph_time_us(lambda i: api.separable(ins[i % 2], outs[i % 2], taps, taps, boundary=api.REPEAT,
+                                                   stream=s), 2, s, 10)
+        res[f"separable9_{name}_8192_repeat"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                                 "achieved_gbs": 2 * es * px / us / 1e3,
+                                                 "frac_hbm": 2 * es * px / us / 1e3 / peak_gbs}
+        us = graph_time_us(lambda i: api.bilateral(ins[i % 2], outs[i % 2], sm, 0.1, boundary=api.REPEAT, stream=s),
+                           2, s, 2)
+        res[f"bilateral13_{name}_8192_repeat"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                                  "exp_per_s": 169 * px / us * 1e6}
+        if dt != torch.float32:
+            us = graph_time_us(lambda i: api.bilateral(ins[i % 2], outs[i % 2], sm, 0.1, boundary=api.REPEAT,
+                                                       fast_weights=True, stream=s), 2, s, 2)
+            res[f"bilateral13_{name}_halfweights_8192_repeat"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                                                  "exp_per_s": 169 * px / us * 1e6}
+        del ins, outs
+    return res
 
 
 def run_e2e(args, L, dev, rank):

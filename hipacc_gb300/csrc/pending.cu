@@ -6,14 +6,6 @@ using namespace hgb;
 
 extern "C" {
 
-int hgb_separable(const hgb_view *, const hgb_view *, const float *, const float *, int, int, float, void *) {
-  return set_error(HGB_ERR_UNSUPPORTED, "hgb_separable: not built");
-}
-
-int hgb_bilateral(const hgb_view *, const hgb_view *, const float *, int, float, int, float, int, void *) {
-  return set_error(HGB_ERR_UNSUPPORTED, "hgb_bilateral: not built");
-}
-
 int hgb_pyramid_plan_create(int, const int *, const int *, int, const float *, int, hgb_pyramid_plan **) {
   return set_error(HGB_ERR_UNSUPPORTED, "hgb_pyramid_plan_create: not built");
 }
