@@ -189,3 +189,66 @@ def last_kernel_timing() -> float:
 
 def autotune(on: bool) -> None:
     L.call("hgb_autotune_enable", 1 if on else 0)
+
+
+class PyramidPlan:
+    """Laplacian pyramids of many FP32 images of uneven sizes (hgb_pyramid_plan)."""
+
+    def __init__(self, widths, heights, levels, mask5, boundary=MIRROR):
+        import numpy as _np
+
+        self.n = len(widths)
+        self.levels = levels
+        w = (C.c_int * self.n)(*[int(v) for v in widths])
+        h = (C.c_int * self.n)(*[int(v) for v in heights])
+        m = _np.ascontiguousarray(mask5, _np.float32)
+        self._h = C.c_void_p()
+        L.call("hgb_pyramid_plan_create", self.n, w, h, levels, m.ctypes.data_as(C.c_void_p), boundary,
+               C.byref(self._h))
+
+    def views(self, image, level):
+        g, lap = L.View(), L.View()
+        L.call("hgb_pyramid_level_view", self._h, image, level, C.byref(g), C.byref(lap))
+        return g, lap
+
+    def _tensor(self, v):
+        # a torch view of device memory owned by the plan (rows padded)
+        import torch
+
+        if not v.data:
+            return None
+        n = v.pitch // 4 * v.height
+        cuda_arr = _DevicePtr(v.data, n * 4)
+        t = torch.as_tensor(cuda_arr, device="cuda").view(torch.float32)
+        return t.view(v.height, v.pitch // 4)[:, :v.width]
+
+    def gauss(self, image, level):
+        return self._tensor(self.views(image, level)[0])
+
+    def lap(self, image, level):
+        return self._tensor(self.views(image, level)[1])
+
+    def decompose(self, mode=0, stream=None):
+        L.call("hgb_pyramid_decompose", self._h, mode, _stream(stream))
+
+    def collapse(self, stream=None):
+        L.call("hgb_pyramid_collapse", self._h, _stream(stream))
+
+    def close(self):
+        if self._h:
+            L.call("hgb_pyramid_plan_destroy", self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _DevicePtr:
+    """__cuda_array_interface__ exporter for plan-owned device memory (bytes)."""
+
+    def __init__(self, ptr, nbytes):
+        self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (int(ptr), False),
+                                         "version": 3, "strides": None}

@@ -1,0 +1,462 @@
+// pyramid.cu -- Laplacian pyramids of many images of uneven sizes.
+//
+// Reference structure (samples-public/5_Other/Gaussian_Laplacian_Pyramid/src/main.cpp:199-248,
+// dsl/pyramid.hpp:97-318): for each level l of each image, three kernels run
+// one after the other, driven by the host's recursive traverse():
+//   blur:        T_l     = conv5x5(G_l) with the boundary mode
+//   subsample:   G_{l+1} = T_l read through a nearest-neighbour accessor
+//                (x = (int)(scale/2 + scale*x'), scale = w_l / w_{l+1},
+//                 lib/AST/Interpolate.cpp:85-113)
+//   difference:  L_l     = G_l - LF(G_{l+1}) (linear filtering accessor with
+//                CLAMP taps, runtime/hipacc_cu_interpolate.hpp:173-216)
+// Level sizes are floor(w / 2^l) (dsl/pyramid.hpp:103-114).
+//
+// GB300 form: one level-tile kernel does all three for a 64 x 32 tile of L_l:
+// it stages the G_l region it needs once in shared memory, evaluates the blur
+// only at the nearest-neighbour sample positions of the G_{l+1} tile plus a
+// one-pixel halo (kept in shared memory), writes the G_{l+1} pixels the tile
+// owns, and writes L_l from the staged G_l and the shared G_{l+1} values.
+// Arithmetic order equals the reference's (blur taps row-major with fused
+// multiply-add; LF as w_a*a, then three fused multiply-adds), so results are
+// bit-identical to the three-kernel program.
+//
+// Launch forms (hgb_pyramid_decompose mode):
+//   0  one persistent launch over a work-list of every level of every image.
+//      CTAs claim tiles in list order (levels ascending) from an atomic
+//      counter; a tile of level l waits (bounded, acquire) until its image's
+//      level l-1 tiles are done, then publishes its own completion (release).
+//      Tiles are claimed in order and only wait on earlier tiles, so resident
+//      CTAs always make progress.
+//   1  one launch per level over all images (the level barrier is the launch
+//      boundary).
+//   2  the reference's launch structure: per image and level, a blur over the
+//      full level, a subsample and a difference launch.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "local_op.cuh"
+#include "tma.cuh"
+
+namespace hgb {
+namespace {
+
+constexpr int PY_TW = 64, PY_TH = 32;              // L_l tile
+constexpr int PY_GW = PY_TW / 2 + 2, PY_GH = PY_TH / 2 + 2;  // G_{l+1} tile + halo
+constexpr int PY_SW = PY_TW + 12, PY_SH = PY_TH + 12;        // staged G_l region bound
+constexpr int PY_THREADS = 256;
+
+struct LevelMeta {
+  float *g;    // Gaussian level
+  float *lap;  // Laplacian level (null for the last level)
+  int w, h;
+  int pitch;   // floats
+  int pad;
+};
+
+struct PyrTile {
+  int img, level, x0, y0;
+};
+
+struct PyrParams {
+  const LevelMeta *meta;  // [img * levels + l]
+  const PyrTile *tiles;
+  int ntiles;
+  int levels;
+  unsigned int *done;       // [img * levels + l]: finished tiles of level l
+  const int *ntiles_il;     // [img * levels + l]: tiles of level l
+  unsigned int *work;       // claim counter (persistent form)
+  int *status;
+  float mask[25];
+  int bmode;
+};
+
+__device__ __forceinline__ float ld_level(const float *p, bool coherent) {
+  // levels written inside the same persistent launch must bypass the
+  // non-coherent read-only path
+  return coherent ? __ldcg(p) : __ldg(p);
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_add(unsigned int *p, unsigned int v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// One 64 x 32 tile of L_level (and the owned part of G_{level+1}).
+__device__ void pyr_tile(const PyrParams &p, const PyrTile t, float *stage, float *gt, bool coherent) {
+  const LevelMeta A = p.meta[t.img * p.levels + t.level];
+  const LevelMeta B = p.meta[t.img * p.levels + t.level + 1];
+  const int wl = A.w, hl = A.h, wn = B.w, hn = B.h;
+  // nearest-neighbour scale G_l -> G_{l+1} and linear-filtering scale G_{l+1} -> L_l
+  const float Sx = (float)wl / (float)wn, Sy = (float)hl / (float)hn;
+  const float sx = (float)wn / (float)wl, sy = (float)hn / (float)hl;
+  const int gx0 = max(0, t.x0 / 2 - 1), gx1 = min(wn, t.x0 / 2 + PY_TW / 2 + 1);
+  const int gy0 = max(0, t.y0 / 2 - 1), gy1 = min(hn, t.y0 / 2 + PY_TH / 2 + 1);
+  auto nn = [](float S, int x, int lim) {
+    int v = (int)__fmaf_rn(S, (float)x, S * 0.5f);
+    return v < lim ? v : lim - 1;
+  };
+  const int rx0 = nn(Sx, gx0, wl) - 2, rx1 = nn(Sx, gx1 - 1, wl) + 3;
+  const int ry0 = nn(Sy, gy0, hl) - 2, ry1 = nn(Sy, gy1 - 1, hl) + 3;
+  const int sw = rx1 - rx0, sh = ry1 - ry0;  // <= PY_SW, PY_SH
+  // ---- stage G_l[ry0..ry1) x [rx0..rx1) through the boundary remap
+  for (int c = threadIdx.x; c < sw * sh; c += PY_THREADS) {
+    const int r = c / sw, q = c - r * sw;
+    int y = ry0 + r, x = rx0 + q;
+    float v;
+    const int yy = remap(p.bmode, y, 0, hl), xx = remap(p.bmode, x, 0, wl);
+    if (yy == (int)0x80000000 || xx == (int)0x80000000)
+      v = 0.0f;
+    else
+      v = ld_level(A.g + (int64_t)yy * A.pitch + xx, coherent);
+    stage[r * PY_SW + q] = v;
+  }
+  __syncthreads();
+  // ---- G_{l+1} on the tile + halo: blur at the nearest-neighbour positions
+  const int gw = gx1 - gx0, gh = gy1 - gy0;
+  for (int c = threadIdx.x; c < gw * gh; c += PY_THREADS) {
+    const int r = c / gw, q = c - r * gw;
+    const int xp = gx0 + q, yp = gy0 + r;
+    const int cx = nn(Sx, xp, wl) - 2 - rx0, cy = nn(Sy, yp, hl) - 2 - ry0;
+    float acc = 0.0f;
+#pragma unroll
+    for (int my = 0; my < 5; ++my)
+#pragma unroll
+      for (int mx = 0; mx < 5; ++mx) acc = __fmaf_rn(p.mask[my * 5 + mx], stage[(cy + my) * PY_SW + cx + mx], acc);
+    gt[r * PY_GW + q] = acc;
+    // owned pixels of G_{l+1}: x' in [x0/2, x0/2 + TW/2), y' likewise
+    if (xp >= t.x0 / 2 && xp < t.x0 / 2 + PY_TW / 2 && yp >= t.y0 / 2 && yp < t.y0 / 2 + PY_TH / 2)
+      B.g[(int64_t)yp * B.pitch + xp] = acc;
+  }
+  __syncthreads();
+  // ---- L_l = G_l - LF(G_{l+1})
+  for (int c = threadIdx.x; c < PY_TW * PY_TH; c += PY_THREADS) {
+    const int r = c / PY_TW, q = c - r * PY_TW;
+    const int x = t.x0 + q, y = t.y0 + r;
+    if (x >= wl || y >= hl) continue;
+    float xb = __fmaf_rn(sx, (float)x, sx * 0.5f) - 0.5f;
+    float yb = __fmaf_rn(sy, (float)y, sy * 0.5f) - 0.5f;
+    xb = xb < 0.0f ? 0.0f : xb;
+    yb = yb < 0.0f ? 0.0f : yb;
+    const int xi = (int)xb, yi = (int)yb;
+    const float xf = xb - (float)xi, yf = yb - (float)yi;
+    const int xa = min(xi, wn - 1) - gx0, xc = min(xi + 1, wn - 1) - gx0;
+    const int ya = min(yi, hn - 1) - gy0, yc = min(yi + 1, hn - 1) - gy0;
+    const float wa = __fmul_rn(1.0f - xf, 1.0f - yf), wb = __fmul_rn(xf, 1.0f - yf);
+    const float wc = __fmul_rn(1.0f - xf, yf), wd = __fmul_rn(xf, yf);
+    float lf = __fmul_rn(wa, gt[ya * PY_GW + xa]);
+    lf = __fmaf_rn(wb, gt[ya * PY_GW + xc], lf);
+    lf = __fmaf_rn(wc, gt[yc * PY_GW + xa], lf);
+    lf = __fmaf_rn(wd, gt[yc * PY_GW + xc], lf);
+    const float g = stage[(y - ry0) * PY_SW + (x - rx0)];
+    A.lap[(int64_t)y * A.pitch + x] = __fsub_rn(g, lf);
+  }
+}
+
+__global__ void __launch_bounds__(PY_THREADS) pyr_level_kernel(const __grid_constant__ PyrParams p, int first) {
+  __shared__ float stage[PY_SW * PY_SH];
+  __shared__ float gt[PY_GW * PY_GH];
+  pyr_tile(p, p.tiles[first + blockIdx.x], stage, gt, false);
+}
+
+__global__ void __launch_bounds__(PY_THREADS) pyr_persistent_kernel(const __grid_constant__ PyrParams p) {
+  __shared__ float stage[PY_SW * PY_SH];
+  __shared__ float gt[PY_GW * PY_GH];
+  __shared__ int s_t;
+  __shared__ int s_ok;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int t = (int)atomicAdd(p.work, 1u);
+      s_t = t;
+      s_ok = 1;
+      if (t < p.ntiles) {
+        const PyrTile tl = p.tiles[t];
+        if (tl.level > 0) {
+          // wait (bounded) until the image's previous level is complete
+          const int k = tl.img * p.levels + tl.level - 1;
+          const unsigned int need = (unsigned int)p.ntiles_il[k];
+          long long spins = 0;
+          while (ld_acquire_u32(&p.done[k]) < need) {
+            if (++spins > kMaxSpins) {
+              s_ok = 0;
+              record_status(p.status, HGB_ERR_TIMEOUT);
+              break;
+            }
+            __nanosleep(64);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const int t = s_t;
+    if (t >= p.ntiles) return;
+    const PyrTile tl = p.tiles[t];
+    if (s_ok) pyr_tile(p, tl, stage, gt, true);
+    __syncthreads();
+    if (threadIdx.x == 0) red_release_add(&p.done[tl.img * p.levels + tl.level], 1u);
+  }
+}
+
+// ---- reference launch structure: difference with a linear-filtering accessor
+__global__ void __launch_bounds__(256) pyr_dog_kernel(LevelMeta A, LevelMeta B) {
+  const int x = blockIdx.x * 64 + (threadIdx.x & 63), y = blockIdx.y * 4 + (threadIdx.x >> 6);
+  if (x >= A.w || y >= A.h) return;
+  const float sx = (float)B.w / (float)A.w, sy = (float)B.h / (float)A.h;
+  float xb = __fmaf_rn(sx, (float)x, sx * 0.5f) - 0.5f;
+  float yb = __fmaf_rn(sy, (float)y, sy * 0.5f) - 0.5f;
+  xb = xb < 0.0f ? 0.0f : xb;
+  yb = yb < 0.0f ? 0.0f : yb;
+  const int xi = (int)xb, yi = (int)yb;
+  const float xf = xb - (float)xi, yf = yb - (float)yi;
+  const int xa = min(xi, B.w - 1), xc = min(xi + 1, B.w - 1), ya = min(yi, B.h - 1), yc = min(yi + 1, B.h - 1);
+  const float wa = __fmul_rn(1.0f - xf, 1.0f - yf), wb = __fmul_rn(xf, 1.0f - yf);
+  const float wc = __fmul_rn(1.0f - xf, yf), wd = __fmul_rn(xf, yf);
+  float lf = __fmul_rn(wa, __ldg(B.g + (int64_t)ya * B.pitch + xa));
+  lf = __fmaf_rn(wb, __ldg(B.g + (int64_t)ya * B.pitch + xc), lf);
+  lf = __fmaf_rn(wc, __ldg(B.g + (int64_t)yc * B.pitch + xa), lf);
+  lf = __fmaf_rn(wd, __ldg(B.g + (int64_t)yc * B.pitch + xc), lf);
+  A.lap[(int64_t)y * A.pitch + x] = __fsub_rn(__ldg(A.g + (int64_t)y * A.pitch + x), lf);
+}
+
+// ---- collapse (Restore): G_l = LF(G_{l+1}) + L_l, one launch per level
+__global__ void __launch_bounds__(256) pyr_restore_kernel(const __grid_constant__ PyrParams p, int first) {
+  const PyrTile t = p.tiles[first + blockIdx.x];
+  const LevelMeta A = p.meta[t.img * p.levels + t.level];
+  const LevelMeta B = p.meta[t.img * p.levels + t.level + 1];
+  const float sx = (float)B.w / (float)A.w, sy = (float)B.h / (float)A.h;
+  for (int c = threadIdx.x; c < PY_TW * PY_TH; c += blockDim.x) {
+    const int x = t.x0 + c % PY_TW, y = t.y0 + c / PY_TW;
+    if (x >= A.w || y >= A.h) continue;
+    float xb = __fmaf_rn(sx, (float)x, sx * 0.5f) - 0.5f;
+    float yb = __fmaf_rn(sy, (float)y, sy * 0.5f) - 0.5f;
+    xb = xb < 0.0f ? 0.0f : xb;
+    yb = yb < 0.0f ? 0.0f : yb;
+    const int xi = (int)xb, yi = (int)yb;
+    const float xf = xb - (float)xi, yf = yb - (float)yi;
+    const int xa = min(xi, B.w - 1), xc = min(xi + 1, B.w - 1), ya = min(yi, B.h - 1), yc = min(yi + 1, B.h - 1);
+    const float wa = __fmul_rn(1.0f - xf, 1.0f - yf), wb = __fmul_rn(xf, 1.0f - yf);
+    const float wc = __fmul_rn(1.0f - xf, yf), wd = __fmul_rn(xf, yf);
+    float lf = __fmul_rn(wa, B.g[(int64_t)ya * B.pitch + xa]);
+    lf = __fmaf_rn(wb, B.g[(int64_t)ya * B.pitch + xc], lf);
+    lf = __fmaf_rn(wc, B.g[(int64_t)yc * B.pitch + xa], lf);
+    lf = __fmaf_rn(wd, B.g[(int64_t)yc * B.pitch + xc], lf);
+    A.g[(int64_t)y * A.pitch + x] = __fadd_rn(lf, A.lap[(int64_t)y * A.pitch + x]);
+  }
+}
+
+}  // namespace
+}  // namespace hgb
+
+using namespace hgb;
+
+struct hgb_pyramid_plan {
+  int n = 0, levels = 0, bmode = 0;
+  float mask[25];
+  std::vector<int> w0, h0;
+  std::vector<LevelMeta> meta;     // host copy
+  std::vector<int> level_first;    // first tile of each level in the list
+  std::vector<int> level_count;
+  void *arena = nullptr;           // all levels of all images
+  void *tmp = nullptr;             // blur buffer of the reference launch structure
+  LevelMeta *d_meta = nullptr;
+  PyrTile *d_tiles = nullptr;
+  int *d_ntiles = nullptr;
+  unsigned int *d_ctrl = nullptr;  // done counters [n*levels] + claim counter
+  int ntiles = 0;
+  int persistent_ctas = 0;
+};
+
+extern "C" {
+
+int hgb_pyramid_plan_create(int n_images, const int *widths, const int *heights, int levels, const float *mask5,
+                            int boundary, hgb_pyramid_plan **out) {
+  HGB_REQUIRE(out && widths && heights && mask5, "hgb_pyramid_plan_create: null argument");
+  HGB_REQUIRE(n_images >= 1 && levels >= 2 && levels <= 16, "hgb_pyramid_plan_create: need >= 1 image, 2..16 levels");
+  HGB_REQUIRE(boundary >= 0 && boundary <= 4, "hgb_pyramid_plan_create: bad boundary");
+  for (int i = 0; i < n_images; ++i)
+    HGB_REQUIRE((widths[i] >> (levels - 1)) >= 1 && (heights[i] >> (levels - 1)) >= 1,
+                "hgb_pyramid_plan_create: pyramid stages too deep for an image size");
+  hgb_pyramid_plan *P = new hgb_pyramid_plan;
+  P->n = n_images;
+  P->levels = levels;
+  P->bmode = boundary;
+  memcpy(P->mask, mask5, sizeof(P->mask));
+  P->w0.assign(widths, widths + n_images);
+  P->h0.assign(heights, heights + n_images);
+  // arena layout: per image, per level: G then L, rows padded to 16 floats
+  size_t bytes = 0, tmp_bytes = 0;
+  std::vector<size_t> goff, loff;
+  P->meta.resize((size_t)n_images * levels);
+  for (int i = 0; i < n_images; ++i) {
+    int w = widths[i], h = heights[i];
+    for (int l = 0; l < levels; ++l) {
+      LevelMeta &m = P->meta[(size_t)i * levels + l];
+      m.w = w;
+      m.h = h;
+      m.pitch = (w + 15) / 16 * 16;
+      goff.push_back(bytes);
+      bytes += (size_t)m.pitch * h * 4;
+      loff.push_back(bytes);
+      if (l + 1 < levels) bytes += (size_t)m.pitch * h * 4;
+      if (l == 0) tmp_bytes = std::max(tmp_bytes, (size_t)m.pitch * h * 4);
+      w /= 2;
+      h /= 2;
+    }
+  }
+  // work-list: levels ascending, then images, then tiles row-major
+  std::vector<PyrTile> tiles;
+  std::vector<int> nil((size_t)n_images * levels, 0);
+  for (int l = 0; l + 1 < levels; ++l) {
+    P->level_first.push_back((int)tiles.size());
+    for (int i = 0; i < n_images; ++i) {
+      const LevelMeta &m = P->meta[(size_t)i * levels + l];
+      for (int y = 0; y < m.h; y += PY_TH)
+        for (int x = 0; x < m.w; x += PY_TW) tiles.push_back(PyrTile{i, l, x, y});
+      nil[(size_t)i * levels + l] = cdiv(m.w, PY_TW) * cdiv(m.h, PY_TH);
+    }
+    P->level_count.push_back((int)tiles.size() - P->level_first.back());
+  }
+  P->ntiles = (int)tiles.size();
+  cudaError_t e = cudaMalloc(&P->arena, bytes);
+  if (e == cudaSuccess) e = cudaMemset(P->arena, 0, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&P->tmp, tmp_bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_meta, P->meta.size() * sizeof(LevelMeta));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_tiles, tiles.size() * sizeof(PyrTile));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_ntiles, nil.size() * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_ctrl, (nil.size() + 1) * sizeof(unsigned int));
+  if (e != cudaSuccess) {
+    hgb_pyramid_plan_destroy(P);
+    return cuda_error(e, "hgb_pyramid_plan_create: allocation");
+  }
+  for (size_t k = 0; k < P->meta.size(); ++k) {
+    P->meta[k].g = (float *)((char *)P->arena + goff[k]);
+    P->meta[k].lap = ((int)(k % levels) + 1 < levels) ? (float *)((char *)P->arena + loff[k]) : nullptr;
+  }
+  e = cudaMemcpy(P->d_meta, P->meta.data(), P->meta.size() * sizeof(LevelMeta), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(P->d_tiles, tiles.data(), tiles.size() * sizeof(PyrTile), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(P->d_ntiles, nil.data(), nil.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    hgb_pyramid_plan_destroy(P);
+    return cuda_error(e, "hgb_pyramid_plan_create: upload");
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pyr_persistent_kernel, PY_THREADS, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  P->persistent_ctas = num_sms() * per_sm;
+  *out = P;
+  return HGB_OK;
+}
+
+int hgb_pyramid_plan_destroy(hgb_pyramid_plan *P) {
+  if (!P) return HGB_OK;
+  cudaFree(P->arena);
+  cudaFree(P->tmp);
+  cudaFree(P->d_meta);
+  cudaFree(P->d_tiles);
+  cudaFree(P->d_ntiles);
+  cudaFree(P->d_ctrl);
+  delete P;
+  return HGB_OK;
+}
+
+int hgb_pyramid_level_view(const hgb_pyramid_plan *P, int image, int level, hgb_view *gauss, hgb_view *lap) {
+  HGB_REQUIRE(P, "hgb_pyramid_level_view: null plan");
+  HGB_REQUIRE(image >= 0 && image < P->n && level >= 0 && level < P->levels, "hgb_pyramid_level_view: bad index");
+  const LevelMeta &m = P->meta[(size_t)image * P->levels + level];
+  hgb_view v;
+  v.dtype = HGB_F32;
+  v.width = m.w;
+  v.height = m.h;
+  v.batch = 1;
+  v.pitch = (int64_t)m.pitch * 4;
+  v.batch_stride = v.pitch * m.h;
+  if (gauss) {
+    *gauss = v;
+    gauss->data = m.g;
+  }
+  if (lap) {
+    *lap = v;
+    lap->data = m.lap;
+  }
+  return HGB_OK;
+}
+
+static void fill_params(const hgb_pyramid_plan *P, PyrParams *p) {
+  memset(p, 0, sizeof(*p));
+  p->meta = P->d_meta;
+  p->tiles = P->d_tiles;
+  p->ntiles = P->ntiles;
+  p->levels = P->levels;
+  p->done = P->d_ctrl;
+  p->ntiles_il = P->d_ntiles;
+  p->work = P->d_ctrl + (size_t)P->n * P->levels;
+  p->status = device_status_word();
+  memcpy(p->mask, P->mask, sizeof(p->mask));
+  p->bmode = P->bmode;
+}
+
+int hgb_pyramid_decompose(hgb_pyramid_plan *P, int mode, void *stream) {
+  HGB_REQUIRE(P, "hgb_pyramid_decompose: null plan");
+  HGB_REQUIRE(mode >= 0 && mode <= 2, "hgb_pyramid_decompose: mode must be 0, 1 or 2");
+  cudaStream_t st = (cudaStream_t)stream;
+  PyrParams p;
+  fill_params(P, &p);
+  if (mode == 0) {
+    HGB_CHECK_CUDA(cudaMemsetAsync(P->d_ctrl, 0, ((size_t)P->n * P->levels + 1) * sizeof(unsigned int), st));
+    const int grid = std::min(P->persistent_ctas, P->ntiles);
+    cudaEvent_t ev = before_launch(st);
+    pyr_persistent_kernel<<<grid, PY_THREADS, 0, st>>>(p);
+    return after_launch("pyr_persistent_kernel", st, ev);
+  }
+  if (mode == 1) {
+    for (int l = 0; l + 1 < P->levels; ++l) {
+      cudaEvent_t ev = before_launch(st);
+      pyr_level_kernel<<<P->level_count[l], PY_THREADS, 0, st>>>(p, P->level_first[l]);
+      const int rc = after_launch("pyr_level_kernel", st, ev);
+      if (rc) return rc;
+    }
+    return HGB_OK;
+  }
+  // mode 2: the reference's kernels, per image and level
+  for (int i = 0; i < P->n; ++i) {
+    for (int l = 0; l + 1 < P->levels; ++l) {
+      const LevelMeta &A = P->meta[(size_t)i * P->levels + l];
+      const LevelMeta &B = P->meta[(size_t)i * P->levels + l + 1];
+      hgb_view ga{A.g, HGB_F32, A.w, A.h, 1, (int64_t)A.pitch * 4, (int64_t)A.pitch * 4 * A.h};
+      hgb_view tv{P->tmp, HGB_F32, A.w, A.h, 1, (int64_t)A.pitch * 4, (int64_t)A.pitch * 4 * A.h};
+      hgb_view gb{B.g, HGB_F32, B.w, B.h, 1, (int64_t)B.pitch * 4, (int64_t)B.pitch * 4 * B.h};
+      int rc = hgb_local_op(&ga, nullptr, &tv, nullptr, P->mask, nullptr, nullptr, 5, 5, HGB_REDUCE_SUM, P->bmode, 0.0f,
+                            stream);
+      if (rc) return rc;
+      rc = hgb_resample(&tv, &gb, 1, stream);
+      if (rc) return rc;
+      cudaEvent_t ev = before_launch(st);
+      pyr_dog_kernel<<<dim3(cdiv(A.w, 64), cdiv(A.h, 4)), 256, 0, st>>>(A, B);
+      rc = after_launch("pyr_dog_kernel", st, ev);
+      if (rc) return rc;
+    }
+  }
+  return HGB_OK;
+}
+
+int hgb_pyramid_collapse(hgb_pyramid_plan *P, void *stream) {
+  HGB_REQUIRE(P, "hgb_pyramid_collapse: null plan");
+  cudaStream_t st = (cudaStream_t)stream;
+  PyrParams p;
+  fill_params(P, &p);
+  for (int l = P->levels - 2; l >= 0; --l) {
+    cudaEvent_t ev = before_launch(st);
+    pyr_restore_kernel<<<P->level_count[l], 256, 0, st>>>(p, P->level_first[l]);
+    const int rc = after_launch("pyr_restore_kernel", st, ev);
+    if (rc) return rc;
+  }
+  return HGB_OK;
+}
+
+}  // extern "C"
