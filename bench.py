@@ -432,6 +432,28 @@ def measure_other_configs(dev, peak_gbs):
             res[f"bilateral13_{name}_halfweights_8192_repeat"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
                                                                   "exp_per_s": 169 * px / us * 1e6}
         del ins, outs
+    del img32
+    # batching: 64 FP32 images, w and h uniform in [257, 4096], 8-level Laplacian pyramid, MIRROR
+    rng = np.random.default_rng(4096)
+    ws_ = rng.integers(257, 4097, 64)
+    hs_ = rng.integers(257, 4097, 64)
+    levels = 8
+    b1 = np.array([1, 4, 6, 4, 1], np.float64) / 16.0
+    plan = api.PyramidPlan(ws_, hs_, levels, np.outer(b1, b1).astype(np.float32), api.MIRROR)
+    for i in range(64):
+        plan.gauss(i, 0).copy_(torch.rand((int(hs_[i]), int(ws_[i])), device=dev))
+    base_px = float(np.sum(ws_.astype(np.int64) * hs_))
+    alg = 0.0
+    for i in range(64):
+        w, h = int(ws_[i]), int(hs_[i])
+        for _ in range(levels - 1):
+            alg += 8.0 * w * h + 4.0 * (w // 2) * (h // 2)  # read G_l, write L_l, write G_{l+1}
+            w, h = w // 2, h // 2
+    for mode, name in ((0, "persistent_1launch"), (1, "per_level_7launches"), (2, "per_image_per_level_1344launches")):
+        us = graph_time_us(lambda i: plan.decompose(mode, stream=s), 1, s, 3 if mode < 2 else 2)
+        res[f"pyramid8_64img_{name}"] = {"us_per_batch": us, "gpix_s": base_px / us / 1e3,
+                                         "achieved_gbs": alg / us / 1e3, "frac_hbm": alg / us / 1e3 / peak_gbs}
+    plan.close()
     return res
 
 

@@ -252,3 +252,23 @@ class _DevicePtr:
     def __init__(self, ptr, nbytes):
         self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (int(ptr), False),
                                          "version": 3, "strides": None}
+
+
+def conv_bilateral_mse(x, t, mask, sigma, smask, boundary=CLAMP, mode=0, stream=None):
+    """Forward + adjoint of y1 = conv7x7(x, mask), y = bilateral9x9(y1; smask,
+    sigma), loss = mean((y - t)^2).  x, t: (B, H, W) float32 CUDA tensors;
+    mask: 7x7 float32 CUDA tensor; sigma: 1-element float32 CUDA tensor.
+    Returns (loss [float64, 1], grad_x, grad_mask [7x7], grad_sigma [1])."""
+    dev = x.device
+    loss = torch.zeros(1, dtype=torch.float64, device=dev)
+    gx = torch.empty_like(x)
+    gm = torch.empty((7, 7), dtype=torch.float32, device=dev)
+    gs = torch.empty(1, dtype=torch.float32, device=dev)
+    sm = np.ascontiguousarray(smask, np.float32)
+    mask = mask.contiguous()
+    vx, vt, vg = view(x), view(t), view(gx)
+    L.call("hgb_conv_bilateral_mse", C.byref(vx), C.byref(vt), C.c_void_p(mask.data_ptr()), 7,
+           sm.ctypes.data_as(C.c_void_p), 9, C.c_void_p(sigma.data_ptr()), boundary, mode,
+           C.c_void_p(loss.data_ptr()), C.byref(vg), C.c_void_p(gm.data_ptr()), C.c_void_p(gs.data_ptr()),
+           _stream(stream))
+    return loss, gx, gm, gs

@@ -1,0 +1,579 @@
+// c5.cu -- forward + adjoint of  y1 = conv(x, mask), y = bilateral(y1; smask,
+// sigma_r), loss = mean((y - t)^2)  over a batch of FP32 images, with the
+// gradients of the loss with respect to x, the mask and sigma_r.
+//
+// Forward semantics: conv as hgb_local_op (row-major taps, fused
+// multiply-add); bilateral as samples-public/3_Preprocessing/Bilateral_Filter
+// (w = smask * exp(-c (y1_q - y1_p)^2), c = 1/(2 sigma_r^2), y = sum w y1_q /
+// sum w) reading y1 through the same boundary mode.  Adjoint (hand-derived,
+// checked against FP64 central differences by the tests):
+//   g_p = 2 (y_p - t_p) / n,  a_p = g_p / W_p
+//   dL/dy1_q += a_p w_po (1 - 2c (y1_q - y_p)(y1_q - y1_p))      (q = r(p+o))
+//   dL/dy1_p += a_p sum_o w_po (y1_q - y_p) 2c (y1_q - y1_p)
+//   dL/dc     = sum_p a_p sum_o w_po (y1_q - y_p) (-(y1_q - y1_p)^2)
+//   dL/dsigma = dL/dc * (-1/sigma^3)
+//   dL/dx_{r(j+o)} += m_o dL/dy1_j,   dL/dm_o = sum_j dL/dy1_j x_{r(j+o)}
+// The boundary is transposed by gathering over pre-images: pixel q collects
+// from every (p, o) with r(p + o) = q, found per axis among the virtual
+// positions within the radius of the border (CLAMP and MIRROR send several
+// virtual positions to an edge pixel; CONSTANT taps carry no gradient).  The
+// bilateral weights are recomputed in the adjoint, never stored.  Inside the
+// image the spatial mask's symmetry makes one exponential serve both the
+// neighbour term (weight of tap o at p = j - o) and the centre term (tap -o
+// at j).  Reductions (loss, dL/dc, dL/dmask) use per-block partials combined
+// in FP64 in block order by the block that takes the last ticket.
+//
+// Launch forms: mode 0 = three batched kernels (forward with the conv
+// recomputed on its halo and the loss gradient in the epilogue, bilateral
+// adjoint, conv adjoint with the mask gradient); mode 1 = the unfused chain
+// per image (conv, bilateral forward, loss gradient, bilateral adjoint without
+// the symmetry reuse, conv adjoint, mask gradient) for comparison.
+// Boundary CLAMP, MIRROR or CONSTANT(0); images at least 8 x 8.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "reduce_common.cuh"
+
+namespace hgb {
+namespace {
+
+constexpr int C5_TW = 32, C5_TH = 16, C5_T = 256;
+constexpr int C5_MK = 7, C5_MR = 3;  // conv mask
+constexpr int C5_BK = 9, C5_BR = 4;  // bilateral
+// staged regions
+constexpr int XS_W = C5_TW + 2 * (C5_MR + C5_BR), XS_H = C5_TH + 2 * (C5_MR + C5_BR);  // x for the fused forward
+constexpr int YS_W = C5_TW + 2 * C5_BR, YS_H = C5_TH + 2 * C5_BR;                      // y1 / a / y (radius 4)
+constexpr int DS_W = C5_TW + 2 * C5_MR, DS_H = C5_TH + 2 * C5_MR;                      // dy1 / x (radius 3)
+
+struct C5Params {
+  const float *x, *t;
+  int64_t xp, tp, xb, tb;  // pitches / batch strides in floats
+  float *y1, *y, *a, *dy1, *dx;
+  int64_t ip, ib;          // pitch / batch stride of the intermediates and dx (floats)
+  int64_t dxp, dxb;
+  int w, h, batch;
+  int bmode;
+  const float *mask_dev;   // 49
+  const float *sigma_dev;  // 1
+  float lsm[C5_BK * C5_BK];  // log2(smask)
+  float sm[C5_BK * C5_BK];
+  double inv_n;            // 1 / (batch * w * h)
+  float2 *loss_part;       // per block Kahan (s, c)
+  float *dc_part;          // per block
+  float *dm_part;          // per block x 49
+  unsigned int *tickets;   // [0] forward, [1] bilateral adjoint, [2] conv adjoint
+  double *loss_dev;
+  float *grad_mask_dev, *grad_sigma_dev;
+  int fuse_conv;           // forward computes y1 from x (else reads y1)
+  int fuse_loss;           // forward writes a (else writes y and W into a)
+  int symmetric;           // bilateral adjoint reuses weights
+  int fuse_dmask;          // conv adjoint accumulates dL/dmask
+  int img_offset;          // image index of blockIdx.z == 0 (per-image launches)
+};
+
+__device__ __forceinline__ float ex2f(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ int remap_c5(int mode, int v, int n) { return remap(mode, v, 0, n); }
+
+__device__ __forceinline__ void sigma_consts(const C5Params &p, float &c, float &k2) {
+  const float s = __ldg(p.sigma_dev);
+  c = 0.5f / (s * s);
+  k2 = -c * 1.4426950408889634f;
+}
+
+// block-wide sum of a float (all threads get nothing; thread 0 returns the value)
+__device__ __forceinline__ float block_sum_f(float v, float *sbuf) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+  if ((threadIdx.x & 31) == 0) sbuf[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float r = 0.0f;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < C5_T / 32; ++i) r += sbuf[i];
+  __syncthreads();
+  return r;
+}
+
+// ------------------------------------------------------------------ forward
+__global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant__ C5Params p) {
+  __shared__ float xs[XS_W * XS_H];
+  __shared__ float ys[YS_W * YS_H];
+  __shared__ float msk[C5_MK * C5_MK];
+  __shared__ float sbuf[32];
+  const int b = blockIdx.z + p.img_offset;
+  const int X0 = blockIdx.x * C5_TW, Y0 = blockIdx.y * C5_TH;
+  const float *x = p.x + (int64_t)b * p.xb;
+  const int W = p.w, H = p.h, bm = p.bmode;
+  for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) msk[i] = __ldg(p.mask_dev + i);
+  if (p.fuse_conv) {
+    constexpr int R = C5_MR + C5_BR;
+    for (int c = threadIdx.x; c < XS_W * XS_H; c += C5_T) {
+      const int r = c / XS_W, q = c - r * XS_W;
+      const int ry = remap_c5(bm, Y0 - R + r, H), rx = remap_c5(bm, X0 - R + q, W);
+      xs[c] = (ry == (int)0x80000000 || rx == (int)0x80000000) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
+    }
+    __syncthreads();
+    // y1 on the tile + bilateral halo; a halo cell outside the image is y1 at
+    // the remapped position (the bilateral reads y1 through the boundary)
+    for (int c = threadIdx.x; c < YS_W * YS_H; c += C5_T) {
+      const int r = c / YS_W, q = c - r * YS_W;
+      const int vy = Y0 - C5_BR + r, vx = X0 - C5_BR + q;
+      const int ry = remap_c5(bm, vy, H), rx = remap_c5(bm, vx, W);
+      float acc = 0.0f;
+      if (ry != (int)0x80000000 && rx != (int)0x80000000) {
+        // staged x coordinate of (ry - 3, rx - 3)
+        const int sy = ry - C5_MR - (Y0 - R), sx = rx - C5_MR - (X0 - R);
+#pragma unroll
+        for (int my = 0; my < C5_MK; ++my)
+#pragma unroll
+          for (int mx = 0; mx < C5_MK; ++mx) acc = __fmaf_rn(msk[my * C5_MK + mx], xs[(sy + my) * XS_W + sx + mx], acc);
+      }
+      ys[c] = acc;
+    }
+  } else {
+    const float *y1 = p.y1 + (int64_t)b * p.ib;
+    for (int c = threadIdx.x; c < YS_W * YS_H; c += C5_T) {
+      const int r = c / YS_W, q = c - r * YS_W;
+      const int ry = remap_c5(bm, Y0 - C5_BR + r, H), rx = remap_c5(bm, X0 - C5_BR + q, W);
+      ys[c] = (ry == (int)0x80000000 || rx == (int)0x80000000) ? 0.0f : __ldg(y1 + (int64_t)ry * p.ip + rx);
+    }
+  }
+  __syncthreads();
+  float c, k2;
+  sigma_consts(p, c, k2);
+  Kahan lsum{0.0f, 0.0f};
+  const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
+  for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
+    const int gx = X0 + tx, gy = Y0 + py;
+    if (gx >= W || gy >= H) continue;
+    const float ctr = ys[(py + C5_BR) * YS_W + tx + C5_BR];
+    float N = 0.0f, Wt = 0.0f;
+#pragma unroll 3
+    for (int oy = 0; oy < C5_BK; ++oy)
+#pragma unroll
+      for (int ox = 0; ox < C5_BK; ++ox) {
+        const float v = ys[(py + oy) * YS_W + tx + ox];
+        const float d = v - ctr;
+        const float wt = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
+        N = __fmaf_rn(wt, v, N);
+        Wt += wt;
+      }
+    const float yv = N / Wt;
+    const int64_t o = (int64_t)b * p.ib + (int64_t)gy * p.ip + gx;
+    if (p.fuse_conv) p.y1[o] = ctr;
+    if (p.fuse_loss) {
+      const float tv = __ldg(p.t + (int64_t)b * p.tb + (int64_t)gy * p.tp + gx);
+      const float e = yv - tv;
+      lsum = kahan_add(lsum, e * e);
+      p.a[o] = (float)(2.0 * (double)e * p.inv_n) / Wt;
+      p.y[o] = yv;
+    } else {
+      p.y[o] = yv;
+      p.a[o] = Wt;  // the unfused chain keeps W and forms a in its own pass
+    }
+  }
+  if (!p.fuse_loss) return;
+  // per-block Kahan partial of the squared error, FP64 combine by the last block
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    Kahan o;
+    o.s = __shfl_down_sync(0xffffffffu, lsum.s, d);
+    o.c = __shfl_down_sync(0xffffffffu, lsum.c, d);
+    lsum = kahan_merge(lsum, o);
+  }
+  __shared__ float2 kp[C5_T / 32];
+  if ((threadIdx.x & 31) == 0) kp[threadIdx.x >> 5] = make_float2(lsum.s, lsum.c);
+  __syncthreads();
+  const unsigned int nb = grid_blocks();
+  if (threadIdx.x == 0) {
+    Kahan k{0.0f, 0.0f};
+    for (int i = 0; i < C5_T / 32; ++i) k = kahan_merge(k, Kahan{kp[i].x, kp[i].y});
+    p.loss_part[block_rank()] = make_float2(k.s, k.c);
+  }
+  if (take_last_ticket(p.tickets + 0)) {
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (unsigned int i = 0; i < nb; ++i) {
+        const float2 v = __ldcg(p.loss_part + i);
+        s += (double)v.x - (double)v.y;
+      }
+      *p.loss_dev = s * p.inv_n;
+      p.tickets[0] = 0u;
+    }
+  }
+}
+
+// unfused chain: a = 2 (y - t) / (n W) and the loss partials, one image
+__global__ void __launch_bounds__(C5_T) c5_alpha_kernel(const __grid_constant__ C5Params p) {
+  const int b = blockIdx.z + p.img_offset;
+  const int gx = blockIdx.x * C5_TW + threadIdx.x % C5_TW;
+  Kahan lsum{0.0f, 0.0f};
+  for (int py = threadIdx.x / C5_TW; py < C5_TH; py += C5_T / C5_TW) {
+    const int gy = blockIdx.y * C5_TH + py;
+    if (gx >= p.w || gy >= p.h) continue;
+    const int64_t o = (int64_t)b * p.ib + (int64_t)gy * p.ip + gx;
+    const float e = p.y[o] - __ldg(p.t + (int64_t)b * p.tb + (int64_t)gy * p.tp + gx);
+    lsum = kahan_add(lsum, e * e);
+    p.a[o] = (float)(2.0 * (double)e * p.inv_n) / p.a[o];
+  }
+  __shared__ float sbuf[32];
+  const float v = block_sum_f(lsum.s - lsum.c, sbuf);
+  if (threadIdx.x == 0) p.loss_part[block_rank() + (unsigned)p.img_offset * grid_blocks()] = make_float2(v, 0.0f);
+}
+
+// ------------------------------------------------------------------ bilateral adjoint
+// per-axis pre-images of index j under the remap, among virtual positions
+// within `rad` of the image: at most 1 + rad entries
+__device__ __forceinline__ int preimages(int mode, int j, int n, int rad, int *out) {
+  int k = 0;
+  out[k++] = j;
+  if (mode == HGB_BOUNDARY_CONSTANT || (j >= rad && j < n - rad)) return k;
+  for (int v = -rad; v < 0; ++v)
+    if (remap(mode, v, 0, n) == j) out[k++] = v;
+  for (int v = n; v < n + rad; ++v)
+    if (remap(mode, v, 0, n) == j) out[k++] = v;
+  return k;
+}
+
+__global__ void __launch_bounds__(C5_T) c5_bilateral_adjoint_kernel(const __grid_constant__ C5Params p) {
+  __shared__ float sa[YS_W * YS_H], sy[YS_W * YS_H], s1[YS_W * YS_H];
+  __shared__ float sbuf[32];
+  const int b = blockIdx.z + p.img_offset;
+  const int X0 = blockIdx.x * C5_TW, Y0 = blockIdx.y * C5_TH;
+  const int W = p.w, H = p.h, bm = p.bmode;
+  const int64_t base = (int64_t)b * p.ib;
+  // in-image cells of [X0-4, X0+TW+4) x [Y0-4, Y0+TH+4); others are never read
+  for (int c = threadIdx.x; c < YS_W * YS_H; c += C5_T) {
+    const int r = c / YS_W, q = c - r * YS_W;
+    const int gy = Y0 - C5_BR + r, gx = X0 - C5_BR + q;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      const int64_t o = base + (int64_t)gy * p.ip + gx;
+      sa[c] = p.a[o];
+      sy[c] = p.y[o];
+      s1[c] = p.y1[o];
+    }
+  }
+  __syncthreads();
+  float c, k2;
+  sigma_consts(p, c, k2);
+  const float c2 = 2.0f * c;
+  float dc = 0.0f;
+  const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
+  auto S = [&](const float *arr, int gy, int gx) { return arr[(gy - Y0 + C5_BR) * YS_W + gx - X0 + C5_BR]; };
+  for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
+    const int jx = X0 + tx, jy = Y0 + py;
+    if (jx >= W || jy >= H) continue;
+    const float aj = S(sa, jy, jx), yj = S(sy, jy, jx), y1j = S(s1, jy, jx);
+    float dn = 0.0f, ctr = 0.0f;
+    const bool inner = jx >= C5_BR && jx < W - C5_BR && jy >= C5_BR && jy < H - C5_BR;
+    if (inner && p.symmetric) {
+#pragma unroll 3
+      for (int oy = 0; oy < C5_BK; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < C5_BK; ++ox) {
+          // p = j - o; tap o of p reads j, tap -o of j reads p; same weight
+          const int qy = jy - (oy - C5_BR), qx = jx - (ox - C5_BR);
+          const float ap = S(sa, qy, qx), ypp = S(sy, qy, qx), y1p = S(s1, qy, qx);
+          const float d = y1j - y1p;
+          const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
+          dn = __fmaf_rn(ap * e, 1.0f - c2 * (y1j - ypp) * d, dn);
+          const float u = e * (y1p - yj);
+          ctr = __fmaf_rn(u, -c2 * d, ctr);  // (y1p - yj) 2c (y1p - y1j)
+          dc = __fmaf_rn(aj * u, -(d * d), dc);
+        }
+    } else {
+      // centre term and dL/dc over j's own taps
+      for (int oy = 0; oy < C5_BK; ++oy)
+        for (int ox = 0; ox < C5_BK; ++ox) {
+          const int qy = remap_c5(bm, jy + oy - C5_BR, H), qx = remap_c5(bm, jx + ox - C5_BR, W);
+          const float v = (qy == (int)0x80000000 || qx == (int)0x80000000) ? 0.0f : S(s1, qy, qx);
+          const float d = v - y1j;
+          const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
+          const float u = e * (v - yj);
+          ctr = __fmaf_rn(u, c2 * d, ctr);
+          dc = __fmaf_rn(aj * u, -(d * d), dc);
+        }
+      // neighbour term gathered over the pre-images of j
+      int prx[1 + C5_BR], pry[1 + C5_BR];
+      const int nx = preimages(bm, jx, W, C5_BR, prx), ny = preimages(bm, jy, H, C5_BR, pry);
+      for (int iy = 0; iy < ny; ++iy)
+        for (int ix = 0; ix < nx; ++ix)
+          for (int oy = 0; oy < C5_BK; ++oy)
+            for (int ox = 0; ox < C5_BK; ++ox) {
+              const int qy = pry[iy] - (oy - C5_BR), qx = prx[ix] - (ox - C5_BR);
+              if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+              const float ap = S(sa, qy, qx), ypp = S(sy, qy, qx), y1p = S(s1, qy, qx);
+              const float d = y1j - y1p;
+              const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
+              dn = __fmaf_rn(ap * e, 1.0f - c2 * (y1j - ypp) * d, dn);
+            }
+    }
+    p.dy1[base + (int64_t)jy * p.ip + jx] = __fmaf_rn(aj, ctr, dn);
+  }
+  const float bdc = block_sum_f(dc, sbuf);
+  const unsigned int nb = grid_blocks();
+  const unsigned int rank = block_rank() + (unsigned)p.img_offset * nb;
+  if (threadIdx.x == 0) p.dc_part[rank] = bdc;
+  if (p.img_offset == 0 && p.batch > 0 && gridDim.z == (unsigned)p.batch) {
+    if (take_last_ticket(p.tickets + 1) && threadIdx.x == 0) {
+      double s = 0.0;
+      for (unsigned int i = 0; i < nb; ++i) s += (double)__ldcg(p.dc_part + i);
+      const double sg = (double)__ldg(p.sigma_dev);
+      *p.grad_sigma_dev = (float)(s * (-1.0 / (sg * sg * sg)));
+      p.tickets[1] = 0u;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ conv adjoint
+__global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_constant__ C5Params p) {
+  __shared__ float sd[DS_W * DS_H], sx[DS_W * DS_H];
+  __shared__ float msk[C5_MK * C5_MK];
+  __shared__ float red[C5_T / 32][C5_MK * C5_MK];
+  const int b = blockIdx.z + p.img_offset;
+  const int X0 = blockIdx.x * C5_TW, Y0 = blockIdx.y * C5_TH;
+  const int W = p.w, H = p.h, bm = p.bmode;
+  const int64_t base = (int64_t)b * p.ib;
+  const float *x = p.x + (int64_t)b * p.xb;
+  for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) msk[i] = __ldg(p.mask_dev + i);
+  for (int c = threadIdx.x; c < DS_W * DS_H; c += C5_T) {
+    const int r = c / DS_W, q = c - r * DS_W;
+    const int gy = Y0 - C5_MR + r, gx = X0 - C5_MR + q;
+    sd[c] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? p.dy1[base + (int64_t)gy * p.ip + gx] : 0.0f;
+    const int ry = remap_c5(bm, gy, H), rx = remap_c5(bm, gx, W);
+    sx[c] = (ry == (int)0x80000000 || rx == (int)0x80000000) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
+  }
+  __syncthreads();
+  auto D = [&](int gy, int gx) { return sd[(gy - Y0 + C5_MR) * DS_W + gx - X0 + C5_MR]; };
+  float dm[C5_MK * C5_MK];
+#pragma unroll
+  for (int i = 0; i < C5_MK * C5_MK; ++i) dm[i] = 0.0f;
+  const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
+  for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
+    const int ix = X0 + tx, iy = Y0 + py;
+    if (ix >= W || iy >= H) continue;
+    float acc = 0.0f;
+    const bool inner = ix >= C5_MR && ix < W - C5_MR && iy >= C5_MR && iy < H - C5_MR;
+    if (inner) {
+#pragma unroll
+      for (int oy = 0; oy < C5_MK; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < C5_MK; ++ox) acc = __fmaf_rn(msk[oy * C5_MK + ox], D(iy - oy + C5_MR, ix - ox + C5_MR), acc);
+    } else {
+      int prx[1 + C5_MR], pry[1 + C5_MR];
+      const int nx = preimages(bm, ix, W, C5_MR, prx), ny = preimages(bm, iy, H, C5_MR, pry);
+      for (int a = 0; a < ny; ++a)
+        for (int c = 0; c < nx; ++c)
+          for (int oy = 0; oy < C5_MK; ++oy)
+            for (int ox = 0; ox < C5_MK; ++ox) {
+              const int jy = pry[a] - (oy - C5_MR), jx = prx[c] - (ox - C5_MR);
+              if (jx < 0 || jx >= W || jy < 0 || jy >= H) continue;
+              acc = __fmaf_rn(msk[oy * C5_MK + ox], D(jy, jx), acc);
+            }
+    }
+    p.dx[(int64_t)b * p.dxb + (int64_t)iy * p.dxp + ix] = acc;
+    if (p.fuse_dmask) {
+      const float dj = D(iy, ix);
+      const bool cst = bm == HGB_BOUNDARY_CONSTANT;
+#pragma unroll
+      for (int oy = 0; oy < C5_MK; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < C5_MK; ++ox) {
+          const int vy = iy + oy - C5_MR, vx = ix + ox - C5_MR;
+          if (cst && (vx < 0 || vx >= W || vy < 0 || vy >= H)) continue;
+          dm[oy * C5_MK + ox] = __fmaf_rn(dj, sx[(vy - Y0 + C5_MR) * DS_W + vx - X0 + C5_MR], dm[oy * C5_MK + ox]);
+        }
+    }
+  }
+  if (!p.fuse_dmask) return;
+  // block partials of dL/dmask (49 values), FP64 combine by the last block
+#pragma unroll
+  for (int i = 0; i < C5_MK * C5_MK; ++i) {
+    float v = dm[i];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][i] = v;
+  }
+  __syncthreads();
+  const unsigned int nb = grid_blocks();
+  const unsigned int rank = block_rank() + (unsigned)p.img_offset * nb;
+  if (threadIdx.x < C5_MK * C5_MK) {
+    float s = 0.0f;
+    for (int wv = 0; wv < C5_T / 32; ++wv) s += red[wv][threadIdx.x];
+    p.dm_part[(size_t)rank * C5_MK * C5_MK + threadIdx.x] = s;
+  }
+  if (p.img_offset == 0 && gridDim.z == (unsigned)p.batch) {
+    if (take_last_ticket(p.tickets + 2)) {
+      if (threadIdx.x < C5_MK * C5_MK) {
+        double s = 0.0;
+        for (unsigned int i = 0; i < nb; ++i) s += (double)__ldcg(p.dm_part + (size_t)i * C5_MK * C5_MK + threadIdx.x);
+        p.grad_mask_dev[threadIdx.x] = (float)s;
+      }
+      if (threadIdx.x == 0) p.tickets[2] = 0u;
+    }
+  }
+}
+
+// unfused chain: the mask gradient as its own pass over one image
+__global__ void __launch_bounds__(C5_T) c5_dmask_kernel(const __grid_constant__ C5Params p) {
+  const int b = blockIdx.z + p.img_offset;
+  const int o = blockIdx.x;  // one mask tap per block row of the grid
+  const int oy = o / C5_MK, ox = o % C5_MK;
+  const int64_t base = (int64_t)b * p.ib;
+  const float *x = p.x + (int64_t)b * p.xb;
+  float s = 0.0f;
+  for (int64_t i = (int64_t)blockIdx.y * C5_T + threadIdx.x; i < (int64_t)p.w * p.h; i += (int64_t)gridDim.y * C5_T) {
+    const int jx = (int)(i % p.w), jy = (int)(i / p.w);
+    const int ry = remap_c5(p.bmode, jy + oy - C5_MR, p.h), rx = remap_c5(p.bmode, jx + ox - C5_MR, p.w);
+    if (ry == (int)0x80000000 || rx == (int)0x80000000) continue;
+    s = __fmaf_rn(p.dy1[base + (int64_t)jy * p.ip + jx], __ldg(x + (int64_t)ry * p.xp + rx), s);
+  }
+  __shared__ float sbuf[32];
+  const float v = block_sum_f(s, sbuf);
+  if (threadIdx.x == 0) p.dm_part[((size_t)p.img_offset * gridDim.y + blockIdx.y) * C5_MK * C5_MK + o] = v;
+}
+
+// unfused chain: final FP64 combines of the per-image partials
+__global__ void c5_combine_kernel(const __grid_constant__ C5Params p, int loss_parts, int dc_parts, int dm_parts) {
+  const int i = threadIdx.x;
+  if (i < C5_MK * C5_MK) {
+    double s = 0.0;
+    for (int k = 0; k < dm_parts; ++k) s += (double)p.dm_part[(size_t)k * C5_MK * C5_MK + i];
+    p.grad_mask_dev[i] = (float)s;
+  }
+  if (i == 64) {
+    double s = 0.0;
+    for (int k = 0; k < loss_parts; ++k) s += (double)p.loss_part[k].x;
+    *p.loss_dev = s * p.inv_n;
+  }
+  if (i == 96) {
+    double s = 0.0;
+    for (int k = 0; k < dc_parts; ++k) s += (double)p.dc_part[k];
+    const double sg = (double)p.sigma_dev[0];
+    *p.grad_sigma_dev = (float)(s * (-1.0 / (sg * sg * sg)));
+  }
+}
+
+}  // namespace
+}  // namespace hgb
+
+using namespace hgb;
+
+extern "C" int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, const float *mask_dev, int mask_k,
+                                      const float *smask, int smask_k, const float *sigma_dev, int boundary, int mode,
+                                      double *loss_dev, const hgb_view *grad_x, float *grad_mask_dev,
+                                      float *grad_sigma_dev, void *stream) {
+  int rc = check_view(x, "x");
+  if (rc) return rc;
+  rc = check_view(t, "t");
+  if (rc) return rc;
+  rc = check_view(grad_x, "grad_x");
+  if (rc) return rc;
+  HGB_REQUIRE(x->dtype == HGB_F32 && t->dtype == HGB_F32 && grad_x->dtype == HGB_F32,
+              "hgb_conv_bilateral_mse: f32 images expected");
+  HGB_REQUIRE(t->width == x->width && t->height == x->height && t->batch == x->batch && grad_x->width == x->width &&
+                  grad_x->height == x->height && grad_x->batch == x->batch,
+              "hgb_conv_bilateral_mse: size mismatch");
+  HGB_REQUIRE(mask_k == C5_MK && smask_k == C5_BK, "hgb_conv_bilateral_mse: built for a 7x7 mask and a 9x9 bilateral");
+  HGB_REQUIRE(mask_dev && smask && sigma_dev && loss_dev && grad_mask_dev && grad_sigma_dev,
+              "hgb_conv_bilateral_mse: null argument");
+  HGB_REQUIRE(boundary == HGB_BOUNDARY_CLAMP || boundary == HGB_BOUNDARY_MIRROR || boundary == HGB_BOUNDARY_CONSTANT,
+              "hgb_conv_bilateral_mse: boundary must be CLAMP, MIRROR or CONSTANT");
+  HGB_REQUIRE(x->width >= 8 && x->height >= 8, "hgb_conv_bilateral_mse: images must be at least 8 x 8");
+  HGB_REQUIRE(mode == 0 || mode == 1, "hgb_conv_bilateral_mse: mode must be 0 (fused) or 1 (unfused)");
+  HGB_REQUIRE(x->pitch % 4 == 0 && t->pitch % 4 == 0 && grad_x->pitch % 4 == 0, "hgb_conv_bilateral_mse: pitches");
+  for (int i = 0; i < C5_BK; ++i)
+    for (int j = 0; j < C5_BK; ++j) {
+      HGB_REQUIRE(smask[i * C5_BK + j] >= 0.0f, "hgb_conv_bilateral_mse: spatial weights must be non-negative");
+      HGB_REQUIRE(smask[i * C5_BK + j] == smask[(C5_BK - 1 - i) * C5_BK + (C5_BK - 1 - j)],
+                  "hgb_conv_bilateral_mse: spatial weights must be point-symmetric");
+    }
+  const int W = x->width, H = x->height, B = x->batch;
+  const int64_t ip = (W + 3) / 4 * 4, ib = ip * H;  // intermediates, floats
+  const dim3 grid(cdiv(W, C5_TW), cdiv(H, C5_TH), B);
+  const size_t nblk = (size_t)grid.x * grid.y * B;
+  const int red_rows = 64;  // row blocks of the unfused mask-gradient pass
+  const size_t nparts = std::max(nblk, (size_t)B * red_rows);
+  // workspace: y1, y, a, dy1 images + partials
+  const size_t img_bytes = (size_t)ib * B * 4;
+  const size_t part_bytes = nparts * (8 + 4 + 4 * C5_MK * C5_MK) + 1024;
+  Workspace ws;
+  rc = workspace_get(4 * img_bytes + part_bytes, &ws);
+  if (rc) return rc;
+  C5Params p;
+  memset(&p, 0, sizeof(p));
+  p.x = (const float *)x->data;
+  p.t = (const float *)t->data;
+  p.xp = x->pitch / 4;
+  p.tp = t->pitch / 4;
+  p.xb = x->batch_stride / 4;
+  p.tb = t->batch_stride / 4;
+  char *wsb = (char *)ws.base;
+  p.y1 = (float *)wsb;
+  p.y = (float *)(wsb + img_bytes);
+  p.a = (float *)(wsb + 2 * img_bytes);
+  p.dy1 = (float *)(wsb + 3 * img_bytes);
+  char *parts = wsb + 4 * img_bytes;
+  p.loss_part = (float2 *)parts;
+  p.dc_part = (float *)(parts + nparts * 8);
+  p.dm_part = (float *)(parts + nparts * 12);
+  p.ip = ip;
+  p.ib = ib;
+  p.dx = (float *)grad_x->data;
+  p.dxp = grad_x->pitch / 4;
+  p.dxb = grad_x->batch_stride / 4;
+  p.w = W;
+  p.h = H;
+  p.batch = B;
+  p.bmode = boundary;
+  p.mask_dev = mask_dev;
+  p.sigma_dev = sigma_dev;
+  for (int i = 0; i < C5_BK * C5_BK; ++i) {
+    p.sm[i] = smask[i];
+    p.lsm[i] = smask[i] > 0.0f ? (float)std::log2((double)smask[i]) : -INFINITY;
+  }
+  p.inv_n = 1.0 / ((double)B * W * H);
+  p.tickets = ws.tickets + 8;
+  p.loss_dev = loss_dev;
+  p.grad_mask_dev = grad_mask_dev;
+  p.grad_sigma_dev = grad_sigma_dev;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t ev = before_launch(st);
+  if (mode == 0) {
+    p.fuse_conv = 1;
+    p.fuse_loss = 1;
+    p.symmetric = 1;
+    p.fuse_dmask = 1;
+    c5_forward_kernel<<<grid, C5_T, 0, st>>>(p);
+    c5_bilateral_adjoint_kernel<<<grid, C5_T, 0, st>>>(p);
+    c5_conv_adjoint_kernel<<<grid, C5_T, 0, st>>>(p);
+    return after_launch("c5 fused", st, ev);
+  }
+  // unfused chain, one image at a time
+  const dim3 g1(grid.x, grid.y, 1);
+  for (int b = 0; b < B; ++b) {
+    hgb_view xv{(void *)(p.x + (int64_t)b * p.xb), HGB_F32, W, H, 1, x->pitch, x->pitch * H};
+    hgb_view yv{p.y1 + (int64_t)b * ib, HGB_F32, W, H, 1, ip * 4, ib * 4};
+    rc = hgb_local_op(&xv, nullptr, &yv, nullptr, nullptr, mask_dev, nullptr, C5_MK, C5_MK, HGB_REDUCE_SUM, boundary,
+                      0.0f, stream);
+    if (rc) return rc;
+    C5Params q = p;
+    q.img_offset = b;
+    q.fuse_conv = 0;
+    q.fuse_loss = 0;
+    q.symmetric = 0;
+    q.fuse_dmask = 0;
+    c5_forward_kernel<<<g1, C5_T, 0, st>>>(q);
+    c5_alpha_kernel<<<g1, C5_T, 0, st>>>(q);
+    c5_bilateral_adjoint_kernel<<<g1, C5_T, 0, st>>>(q);
+    c5_conv_adjoint_kernel<<<g1, C5_T, 0, st>>>(q);
+    c5_dmask_kernel<<<dim3(C5_MK * C5_MK, red_rows, 1), C5_T, 0, st>>>(q);
+  }
+  c5_combine_kernel<<<1, 128, 0, st>>>(p, (int)nblk, (int)nblk, B * red_rows);
+  return after_launch("c5 unfused", st, ev);
+}

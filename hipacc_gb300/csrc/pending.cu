@@ -11,9 +11,4 @@ int hgb_local_op_adjoint(const hgb_view *, const hgb_view *, const hgb_view *, c
   return set_error(HGB_ERR_UNSUPPORTED, "hgb_local_op_adjoint: not built");
 }
 
-int hgb_conv_bilateral_mse(const hgb_view *, const hgb_view *, const float *, int, const float *, int, const float *,
-                           int, int, double *, const hgb_view *, float *, float *, void *) {
-  return set_error(HGB_ERR_UNSUPPORTED, "hgb_conv_bilateral_mse: not built");
-}
-
 }  // extern "C"

@@ -1,0 +1,120 @@
+"""GPU forward + adjoint of conv7x7 -> bilateral9x9 -> MSE against the FP64
+oracle (hand adjoint, itself pinned to FP64 central differences) and FP64
+central differences (eps = 1e-4) on 64x64 crops.  Tolerances: the kernels
+evaluate the range weights with the FP32 exp2 instruction and accumulate in
+FP32, so gradients agree with FP64 to ADJ_TOL relative (L2 norm) and the
+loss to LOSS_TOL."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+ADJ_TOL = 2e-3
+LOSS_TOL = 1e-4
+
+
+def _setup(oracle, B, H, W, boundary, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.random((B, H, W), dtype=np.float32)
+    g15 = oracle.gaussian_mask(7, 1.5)
+    t = np.stack([oracle.local_op(x[i], mask=g15, boundary=boundary) for i in range(B)]).astype(np.float32)
+    mask = rng.normal(0, 0.02, (7, 7)).astype(np.float32)
+    mask[3, 3] += 0.8  # a trained-like mask so that y1 is not near zero
+    sm = oracle.spatial_mask(9, 2.0)
+    return x, t, mask, sm
+
+
+def _gpu(api, x, t, mask, sigma, sm, boundary, mode):
+    loss, gx, gm, gs = api.conv_bilateral_mse(torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda(),
+                                              torch.from_numpy(mask).cuda(),
+                                              torch.tensor([sigma], dtype=torch.float32, device="cuda"), sm, boundary,
+                                              mode)
+    torch.cuda.synchronize()
+    return float(loss.item()), gx.cpu().numpy(), gm.cpu().numpy(), float(gs.item())
+
+
+def _oracle_batch(oracle, x, t, mask, sm, sigma, boundary):
+    """The batch loss is the mean over every pixel of every image."""
+    B = x.shape[0]
+    L, dx, dm, ds = 0.0, [], np.zeros((7, 7)), 0.0
+    for i in range(B):
+        l, a, b, c = oracle.c5_grad(x[i], t[i], mask.astype(np.float64), sm.astype(np.float64), sigma, boundary)
+        L += l / B
+        dx.append(a / B)
+        dm += b / B
+        ds += c / B
+    return L, np.stack(dx), dm, ds
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-30))
+
+
+@pytest.mark.parametrize("boundary", [1, 3, 4])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_adjoint_vs_fp64_oracle(gpu, oracle, boundary, mode):
+    x, t, mask, sm = _setup(oracle, 2, 64, 64, boundary, 10 + boundary)
+    sigma = 0.15
+    L, dx, dm, ds = _gpu(gpu, x, t, mask, sigma, sm, boundary, mode)
+    L0, dx0, dm0, ds0 = _oracle_batch(oracle, x, t, mask, sm, sigma, boundary)
+    assert abs(L - L0) <= LOSS_TOL * abs(L0)
+    assert rel(dx, dx0) <= ADJ_TOL, rel(dx, dx0)
+    assert rel(dm, dm0) <= ADJ_TOL, rel(dm, dm0)
+    assert abs(ds - ds0) <= ADJ_TOL * abs(ds0), (ds, ds0)
+
+
+@pytest.mark.parametrize("boundary", [1, 3])
+def test_adjoint_vs_central_differences(gpu, oracle, boundary):
+    """FP64 central differences (eps = 1e-4) of the FP64 forward on a 64x64 crop."""
+    x, t, mask, sm = _setup(oracle, 1, 64, 64, boundary, 20 + boundary)
+    sigma = 0.15
+    _, dx, dm, ds = _gpu(gpu, x, t, mask, sigma, sm, boundary, 0)
+    eps = 1e-4
+    x64, t64, m64, s64 = x[0].astype(np.float64), t[0].astype(np.float64), mask.astype(np.float64), sm.astype(np.float64)
+    f = lambda xx, mm, ss: oracle.c5_loss(xx, t64, mm, s64, ss, boundary)
+    for (i, j) in [(0, 0), (0, 63), (63, 5), (31, 32), (2, 61)]:
+        xp, xm = x64.copy(), x64.copy()
+        xp[i, j] += eps
+        xm[i, j] -= eps
+        fd = (f(xp, m64, sigma) - f(xm, m64, sigma)) / (2 * eps)
+        assert abs(dx[0, i, j] - fd) <= 5e-3 * max(abs(fd), 1e-6) + 1e-9, (i, j, dx[0, i, j], fd)
+    for (i, j) in [(0, 0), (3, 3), (6, 2)]:
+        mp, mm = m64.copy(), m64.copy()
+        mp[i, j] += eps
+        mm[i, j] -= eps
+        fd = (f(x64, mp, sigma) - f(x64, mm, sigma)) / (2 * eps)
+        assert abs(dm[i, j] - fd) <= 5e-3 * abs(fd), (i, j, dm[i, j], fd)
+    fd = (f(x64, m64, sigma + eps) - f(x64, m64, sigma - eps)) / (2 * eps)
+    assert abs(ds - fd) <= 5e-3 * abs(fd), (ds, fd)
+
+
+def test_fused_equals_unfused(gpu, oracle):
+    x, t, mask, sm = _setup(oracle, 3, 96, 160, 3, 30)
+    a = _gpu(gpu, x, t, mask, 0.15, sm, 3, 0)
+    b = _gpu(gpu, x, t, mask, 0.15, sm, 3, 1)
+    assert abs(a[0] - b[0]) <= 1e-6 * abs(b[0])
+    assert rel(a[1], b[1]) <= 1e-5 and rel(a[2], b[2]) <= 1e-5 and abs(a[3] - b[3]) <= 1e-5 * abs(b[3])
+
+
+def test_autograd_wrapper(gpu, oracle):
+    from hipacc_gb300.autograd import ConvBilateralMSE
+
+    x, t, mask, sm = _setup(oracle, 1, 48, 40, 1, 40)
+    xt = torch.from_numpy(x).cuda().requires_grad_(True)
+    mt = torch.from_numpy(mask).cuda().requires_grad_(True)
+    st = torch.tensor([0.15], device="cuda", requires_grad=True)
+    loss = ConvBilateralMSE.apply(xt, torch.from_numpy(t).cuda(), mt, st, sm, 1)
+    (2.0 * loss).backward()
+    _, dx, dm, ds = _gpu(gpu, x, t, mask, 0.15, sm, 1, 0)
+    assert np.allclose(xt.grad.cpu().numpy(), 2 * dx) and np.allclose(mt.grad.cpu().numpy(), 2 * dm)
+    assert abs(st.grad.item() - 2 * ds) <= 1e-6 * abs(ds)
+
+
+def test_adjoint_2048(gpu, oracle):
+    """One 2048x2048 image of the differentiation workload against FP64."""
+    x, t, mask, sm = _setup(oracle, 1, 2048, 2048, 3, 50)
+    L, dx, dm, ds = _gpu(gpu, x, t, mask, 0.15, sm, 3, 0)
+    L0, dx0, dm0, ds0 = _oracle_batch(oracle, x, t, mask, sm, 0.15, 3)
+    assert abs(L - L0) <= LOSS_TOL * abs(L0)
+    assert rel(dx, dx0) <= ADJ_TOL and rel(dm, dm0) <= ADJ_TOL and abs(ds - ds0) <= ADJ_TOL * abs(ds0)
