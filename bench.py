@@ -454,6 +454,25 @@ def measure_other_configs(dev, peak_gbs):
         res[f"pyramid8_64img_{name}"] = {"us_per_batch": us, "gpix_s": base_px / us / 1e3,
                                          "achieved_gbs": alg / us / 1e3, "frac_hbm": alg / us / 1e3 / peak_gbs}
     plan.close()
+    # differentiation: 16 x 2048^2, learnable 7x7 mask + 9x9 bilateral (sigma_d = 2) with learnable sigma_r
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    x = torch.rand((16, 2048, 2048), device=dev, generator=g)
+    ax = np.arange(-3, 4, dtype=np.float64)
+    g15 = np.exp(-(ax[None, :] ** 2 + ax[:, None] ** 2) / (2 * 1.5 * 1.5))
+    g15 = (g15 / g15.sum()).astype(np.float32)
+    t = torch.empty_like(x)
+    api.local_op(x, t, mask=g15, boundary=api.CLAMP)
+    mask = (torch.randn((7, 7), device=dev, generator=g) * 0.02).contiguous()
+    sigma = torch.tensor([0.15], device=dev)
+    ax9 = np.arange(-4, 5, dtype=np.float64)
+    sm9 = np.exp(-(ax9[None, :] ** 2 + ax9[:, None] ** 2) / (2 * 4.0)).astype(np.float32)
+    px = 16 * 2048 * 2048
+    for mode, name in ((0, "fused_3launches"), (1, "unfused_per_image")):
+        us = graph_time_us(lambda i: api.conv_bilateral_mse(x, t, mask, sigma, sm9, api.CLAMP, mode, stream=s), 1, s,
+                           3)
+        res[f"conv7_bilateral9_mse_fwd_adj_16x2048_{name}"] = {"us_per_batch": us, "gpix_s": px / us / 1e3}
+    del x, t
     return res
 
 

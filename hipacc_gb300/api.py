@@ -272,3 +272,24 @@ def conv_bilateral_mse(x, t, mask, sigma, smask, boundary=CLAMP, mode=0, stream=
            C.c_void_p(loss.data_ptr()), C.byref(vg), C.c_void_p(gm.data_ptr()), C.c_void_p(gs.data_ptr()),
            _stream(stream))
     return loss, gx, gm, gs
+
+
+def local_op_adjoint(grad_out, mask, boundary=CLAMP, inp=None, want_grad_in=True, want_grad_mask=True, stream=None):
+    """Adjoint of the SUM local operator: (grad_in, grad_mask) for a host mask
+    (2-D array) or a device mask (2-D float32 CUDA tensor)."""
+    gi = torch.empty_like(grad_out) if want_grad_in else None
+    if torch.is_tensor(mask):
+        mh, mw = mask.shape
+        m_host, m_dev = None, C.c_void_p(mask.contiguous().data_ptr())
+    else:
+        m = np.ascontiguousarray(mask, np.float32)
+        mh, mw = m.shape
+        m_host, m_dev = m.ctypes.data_as(C.c_void_p), None
+    gm = torch.empty((mh, mw), dtype=torch.float32, device=grad_out.device) if want_grad_mask else None
+    vg = view(grad_out)
+    vi = view(inp) if inp is not None else None
+    vgi = view(gi) if gi is not None else None
+    L.call("hgb_local_op_adjoint", None if vi is None else C.byref(vi), C.byref(vg),
+           None if vgi is None else C.byref(vgi), m_host, m_dev, mw, mh, boundary,
+           None if gm is None else C.c_void_p(gm.data_ptr()), _stream(stream))
+    return gi, gm

@@ -1,0 +1,206 @@
+// local_adjoint.cu -- hgb_local_op_adjoint: the adjoint of the SUM local
+// operator out(j) = sum_o m_o in(r(j + o)) (r = boundary remap,
+// lib/AST/BorderHandling.cpp:41-120; tap offsets o = (mx - mw/2, my - mh/2)).
+//   grad_in(i)  = sum over (j, o) with r(j + o) = i of m_o grad_out(j)
+//   grad_m(o)   = sum_j grad_out(j) in(r(j + o))
+// CONSTANT taps read the constant, which carries no gradient.  The boundary is
+// transposed by gathering over the pre-images of i under r: for pixels far
+// from the border the only pre-image is i itself (grad_in is the correlation
+// with the flipped mask, staged in shared memory); near the border every
+// virtual position within the mask radius that r sends to i contributes
+// (CLAMP: all positions beyond the edge, MIRROR: the reflected one, REPEAT: the
+// wrapped ones).  grad_m is reduced per tap over row blocks and combined in
+// FP64 in a fixed order, so it is deterministic.  FP32 storage.
+#include <cstring>
+
+#include "reduce_common.cuh"
+
+namespace hgb {
+namespace {
+
+constexpr int LA_TW = 32, LA_TH = 16, LA_T = 256, LA_MAX = 15;
+constexpr int LA_SW = LA_TW + 2 * LA_MAX, LA_SH = LA_TH + 2 * LA_MAX;
+constexpr int LA_ROWBLOCKS = 64;
+
+struct AdjParams {
+  const float *in, *gout;
+  float *gin;
+  int64_t in_p, gout_p, gin_p, in_b, gout_b, gin_b;  // floats
+  int w, h, batch;
+  int mw, mh, bmode;
+  const float *mask_dev;
+  float mask[LA_MAX * LA_MAX];
+  float *part;          // [taps][batch * LA_ROWBLOCKS]
+  float *grad_mask_dev;
+};
+
+__device__ __forceinline__ int pre_list(int mode, int i, int n, int lo_off, int hi_off, int *out) {
+  // virtual v with r(v) == i among [-hi_off, n + lo_off): the positions a tap
+  // can reach from inside the image
+  int k = 0;
+  out[k++] = i;
+  if (mode == HGB_BOUNDARY_CONSTANT) return k;
+  for (int v = -hi_off; v < 0; ++v)
+    if (remap(mode, v, 0, n) == i && k < 2 * LA_MAX + 1) out[k++] = v;
+  for (int v = n; v < n + lo_off; ++v)
+    if (remap(mode, v, 0, n) == i && k < 2 * LA_MAX + 1) out[k++] = v;
+  return k;
+}
+
+__global__ void __launch_bounds__(LA_T) adj_in_kernel(const __grid_constant__ AdjParams p) {
+  __shared__ float sg[LA_SW * LA_SH];
+  __shared__ float msk[LA_MAX * LA_MAX];
+  const int b = blockIdx.z;
+  const int X0 = blockIdx.x * LA_TW, Y0 = blockIdx.y * LA_TH;
+  const int mw = p.mw, mh = p.mh, rxl = mw / 2, ryl = mh / 2, rxh = mw - 1 - rxl, ryh = mh - 1 - ryl;
+  const float *gout = p.gout + (int64_t)b * p.gout_b;
+  for (int k = threadIdx.x; k < mw * mh; k += LA_T) msk[k] = p.mask_dev ? __ldg(p.mask_dev + k) : p.mask[k];
+  // grad_out over [X0 - rxh, X0 + TW + rxl) x [Y0 - ryh, Y0 + TH + ryl), zero outside the image
+  const int sw = LA_TW + mw - 1, sh = LA_TH + mh - 1;
+  for (int c = threadIdx.x; c < sw * sh; c += LA_T) {
+    const int r = c / sw, q = c - r * sw;
+    const int gy = Y0 - ryh + r, gx = X0 - rxh + q;
+    sg[r * LA_SW + q] = (gx >= 0 && gx < p.w && gy >= 0 && gy < p.h) ? __ldg(gout + (int64_t)gy * p.gout_p + gx) : 0.0f;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % LA_TW, ty = threadIdx.x / LA_TW;
+  for (int py = ty; py < LA_TH; py += LA_T / LA_TW) {
+    const int ix = X0 + tx, iy = Y0 + py;
+    if (ix >= p.w || iy >= p.h) continue;
+    float acc = 0.0f;
+    // pixels with no pre-image besides themselves: farther than the larger
+    // reach of the mask from every border
+    const int rx = max(rxl, rxh), ry = max(ryl, ryh);
+    const bool inner = ix >= rx && ix < p.w - rx && iy >= ry && iy < p.h - ry;
+    if (inner) {
+      // j = i - o for every tap (mask flipped), rows and columns ascending in o
+      for (int my = 0; my < mh; ++my)
+        for (int mx = 0; mx < mw; ++mx) {
+          const int jy = iy - (my - ryl), jx = ix - (mx - rxl);
+          acc = __fmaf_rn(msk[my * mw + mx], sg[(jy - Y0 + ryh) * LA_SW + (jx - X0 + rxh)], acc);
+        }
+    } else {
+      int prx[2 * LA_MAX + 1], pry[2 * LA_MAX + 1];
+      const int nx = pre_list(p.bmode, ix, p.w, rxl + 1, rxh + 1, prx);
+      const int ny = pre_list(p.bmode, iy, p.h, ryl + 1, ryh + 1, pry);
+      for (int a = 0; a < ny; ++a)
+        for (int c = 0; c < nx; ++c)
+          for (int my = 0; my < mh; ++my)
+            for (int mx = 0; mx < mw; ++mx) {
+              const int jy = pry[a] - (my - ryl), jx = prx[c] - (mx - rxl);
+              if (jx < 0 || jx >= p.w || jy < 0 || jy >= p.h) continue;
+              acc = __fmaf_rn(msk[my * mw + mx], __ldg(gout + (int64_t)jy * p.gout_p + jx), acc);
+            }
+    }
+    p.gin[(int64_t)b * p.gin_b + (int64_t)iy * p.gin_p + ix] = acc;
+  }
+}
+
+// grid (taps, LA_ROWBLOCKS, batch): partial of grad_m(o) over a band of rows
+__global__ void __launch_bounds__(LA_T) adj_mask_kernel(const __grid_constant__ AdjParams p) {
+  const int o = blockIdx.x, b = blockIdx.z;
+  const int my = o / p.mw, mx = o - my * p.mw;
+  const int oy = my - p.mh / 2, ox = mx - p.mw / 2;
+  const float *in = p.in + (int64_t)b * p.in_b;
+  const float *gout = p.gout + (int64_t)b * p.gout_b;
+  float s = 0.0f;
+  for (int y = blockIdx.y; y < p.h; y += gridDim.y) {
+    const int ry = remap(p.bmode, y + oy, 0, p.h);
+    if (ry == (int)0x80000000) continue;
+    for (int x = threadIdx.x; x < p.w; x += LA_T) {
+      const int rx = remap(p.bmode, x + ox, 0, p.w);
+      if (rx == (int)0x80000000) continue;
+      s = __fmaf_rn(__ldg(gout + (int64_t)y * p.gout_p + x), __ldg(in + (int64_t)ry * p.in_p + rx), s);
+    }
+  }
+  __shared__ float sb[LA_T / 32];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(0xffffffffu, s, d);
+  if ((threadIdx.x & 31) == 0) sb[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int i = 0; i < LA_T / 32; ++i) t += sb[i];
+    p.part[(size_t)o * gridDim.y * gridDim.z + (size_t)b * gridDim.y + blockIdx.y] = t;
+  }
+}
+
+__global__ void adj_mask_combine(const __grid_constant__ AdjParams p, int nparts) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= p.mw * p.mh) return;
+  double s = 0.0;
+  for (int k = 0; k < nparts; ++k) s += (double)p.part[(size_t)o * nparts + k];
+  p.grad_mask_dev[o] = (float)s;
+}
+
+}  // namespace
+}  // namespace hgb
+
+using namespace hgb;
+
+extern "C" int hgb_local_op_adjoint(const hgb_view *in, const hgb_view *grad_out, const hgb_view *grad_in,
+                                    const float *mask, const float *mask_dev, int mask_w, int mask_h, int boundary,
+                                    float *grad_mask_dev, void *stream) {
+  int rc = check_view(grad_out, "grad_out");
+  if (rc) return rc;
+  HGB_REQUIRE(grad_out->dtype == HGB_F32, "hgb_local_op_adjoint: f32 storage expected");
+  HGB_REQUIRE(mask_w >= 1 && mask_h >= 1 && mask_w <= LA_MAX && mask_h <= LA_MAX,
+              "hgb_local_op_adjoint: mask size must be 1..15");
+  HGB_REQUIRE((mask != nullptr) != (mask_dev != nullptr), "hgb_local_op_adjoint: give exactly one of mask, mask_dev");
+  HGB_REQUIRE(boundary >= 0 && boundary <= 4, "hgb_local_op_adjoint: bad boundary");
+  HGB_REQUIRE(grad_in || grad_mask_dev, "hgb_local_op_adjoint: nothing to compute");
+  if (grad_in) {
+    rc = check_view(grad_in, "grad_in");
+    if (rc) return rc;
+    HGB_REQUIRE(grad_in->dtype == HGB_F32 && grad_in->width == grad_out->width &&
+                    grad_in->height == grad_out->height && grad_in->batch == grad_out->batch,
+                "hgb_local_op_adjoint: grad_in must match grad_out");
+  }
+  if (grad_mask_dev) {
+    rc = check_view(in, "in");
+    if (rc) return rc;
+    HGB_REQUIRE(in->dtype == HGB_F32 && in->width == grad_out->width && in->height == grad_out->height &&
+                    in->batch == grad_out->batch,
+                "hgb_local_op_adjoint: in must match grad_out");
+  }
+  AdjParams p;
+  memset(&p, 0, sizeof(p));
+  p.gout = (const float *)grad_out->data;
+  p.gout_p = grad_out->pitch / 4;
+  p.gout_b = grad_out->batch_stride / 4;
+  if (in) {
+    p.in = (const float *)in->data;
+    p.in_p = in->pitch / 4;
+    p.in_b = in->batch_stride / 4;
+  }
+  if (grad_in) {
+    p.gin = (float *)grad_in->data;
+    p.gin_p = grad_in->pitch / 4;
+    p.gin_b = grad_in->batch_stride / 4;
+  }
+  p.w = grad_out->width;
+  p.h = grad_out->height;
+  p.batch = grad_out->batch;
+  p.mw = mask_w;
+  p.mh = mask_h;
+  p.bmode = boundary;
+  p.mask_dev = mask_dev;
+  if (mask)
+    for (int i = 0; i < mask_w * mask_h; ++i) p.mask[i] = mask[i];
+  p.grad_mask_dev = grad_mask_dev;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t ev = before_launch(st);
+  if (grad_in) {
+    adj_in_kernel<<<dim3(cdiv(p.w, LA_TW), cdiv(p.h, LA_TH), p.batch), LA_T, 0, st>>>(p);
+  }
+  if (grad_mask_dev) {
+    const int taps = mask_w * mask_h, nparts = LA_ROWBLOCKS * p.batch;
+    Workspace ws;
+    rc = workspace_get((size_t)taps * nparts * 4 + 64, &ws);
+    if (rc) return rc;
+    p.part = (float *)ws.base;
+    adj_mask_kernel<<<dim3(taps, LA_ROWBLOCKS, p.batch), LA_T, 0, st>>>(p);
+    adj_mask_combine<<<cdiv(taps, 128), 128, 0, st>>>(p, nparts);
+  }
+  return after_launch("local_op_adjoint", st, ev);
+}

@@ -1,0 +1,59 @@
+"""GPU adjoint of the SUM local operator against an FP64 scatter restatement:
+every tap o of every output j sends m_o * grad_out(j) to r(j + o) (CONSTANT
+taps send nothing), and grad_m(o) = sum_j grad_out(j) in(r(j + o))."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def remap_vec(oracle, mode, idx, n):
+    return np.array([oracle.remap(mode, int(i), 0, n) for i in idx], np.int64)
+
+
+def scatter_adjoint(oracle, img, gout, mask, mode):
+    h, w = gout.shape
+    mh, mw = mask.shape
+    gin = np.zeros((h, w))
+    gm = np.zeros((mh, mw))
+    ys, xs = np.arange(h), np.arange(w)
+    for my in range(mh):
+        ry = remap_vec(oracle, mode, ys + my - mh // 2, h)
+        for mx in range(mw):
+            rx = remap_vec(oracle, mode, xs + mx - mw // 2, w)
+            oky, okx = ry >= 0, rx >= 0
+            Y, X = np.meshgrid(np.where(oky)[0], np.where(okx)[0], indexing="ij")
+            np.add.at(gin, (ry[Y], rx[X]), mask[my, mx] * gout[Y, X])
+            gm[my, mx] = np.sum(gout[Y, X] * img[ry[Y], rx[X]])
+    return gin, gm
+
+
+@pytest.mark.parametrize("shape", [(3, 3), (5, 5), (7, 7), (4, 6), (1, 9)])
+@pytest.mark.parametrize("mode", [1, 2, 3, 4])
+def test_local_adjoint(gpu, oracle, shape, mode):
+    rng = np.random.default_rng(hash((shape, mode)) % 2**32)
+    h, w = 37, 53
+    img = rng.random((h, w)).astype(np.float32)
+    gout = rng.normal(0, 1, (h, w)).astype(np.float32)
+    mask = rng.normal(0, 1, shape).astype(np.float32)
+    gi, gm = gpu.local_op_adjoint(torch.from_numpy(gout).cuda(), mask, mode, inp=torch.from_numpy(img).cuda())
+    torch.cuda.synchronize()
+    rgi, rgm = scatter_adjoint(oracle, img.astype(np.float64), gout.astype(np.float64), mask.astype(np.float64), mode)
+    assert np.max(np.abs(gi.cpu().numpy() - rgi)) <= 1e-4 * max(1.0, np.max(np.abs(rgi)))
+    assert np.max(np.abs(gm.cpu().numpy() - rgm)) <= 1e-4 * max(1.0, np.max(np.abs(rgm)))
+
+
+def test_local_adjoint_is_transpose(gpu, oracle):
+    """<conv(x), g> == <x, conv^T(g)> for every boundary with a device mask."""
+    rng = np.random.default_rng(3)
+    x = rng.random((2, 40, 50)).astype(np.float32)
+    g = rng.normal(0, 1, (2, 40, 50)).astype(np.float32)
+    m = rng.normal(0, 1, (5, 5)).astype(np.float32)
+    for mode in (1, 2, 3, 4):
+        xt, gt = torch.from_numpy(x).cuda(), torch.from_numpy(g).cuda()
+        y = gpu.local_op(xt, mask=m, boundary=mode, const=0.0)
+        gi, _ = gpu.local_op_adjoint(gt, torch.from_numpy(m).cuda(), mode, want_grad_mask=False)
+        lhs = float((y.double() * gt.double()).sum())
+        rhs = float((xt.double() * gi.double()).sum())
+        assert abs(lhs - rhs) <= 1e-4 * abs(lhs), (mode, lhs, rhs)
