@@ -60,7 +60,10 @@ def build(verbose: bool = False, ptxas_info: bool = False, jobs: int | None = No
             if log:
                 sys.stdout.write(log)
     if _stale(LIB, objs):
-        cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        # the runtime library's directory is recorded so that plain C++ hosts
+        # (no Python process that already loaded it) find it too
+        cudart_dir = os.path.join(os.path.dirname(os.path.dirname(cc)), "lib64")
+        cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-Xlinker", "-rpath", "-Xlinker", cudart_dir]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -75,3 +75,15 @@ def test_missing_library_fails_loudly(tmp_path):
             L.load(str(tmp_path / "nope.so"))
     finally:
         L._lib = saved
+
+
+def test_samples_compile_and_link(hgb_lib, tmp_path):
+    """The C++ host surface compiles and links against the library (CPU only)."""
+    import subprocess
+
+    lib = os.path.join(ROOT, "hipacc_gb300")
+    for name in ("gaussian_blur", "sobel", "color_reduce", "pyramid", "bilateral"):
+        r = subprocess.run(["g++", "-O1", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                            os.path.join(ROOT, "tests", "samples", name + ".cpp"), "-L", lib, "-lhipacc_gb300",
+                            "-Wl,-rpath," + lib, "-o", str(tmp_path / name)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
