@@ -8,8 +8,9 @@ image pairs (NSETS x 117 MB, several times the 129 MB L2), so every step reads
 its inputs from HBM.  Steps are replayed from CUDA graphs.
 
 Metric: Gpixels/s = (Sobel pixels + gray pixels) per second, whole job.
-`roofline` is for the dominant kernel (the gray point operator, 5 algorithmic
-bytes per pixel); `kernels` lists both kernels' achieved HBM bandwidth.
+`roofline` is for the dominant kernel (the one with the longer launch: Sobel at
+2 algorithmic bytes per pixel or gray at 5); `kernels` lists both kernels'
+achieved HBM bandwidth.
 `e2e` drives the same step through the C ABI with host buffers
 (hgb_image_write / kernels / hgb_image_read): pinned host -> device copies of
 both inputs and device -> host reads of both outputs and the two scalars.
@@ -38,6 +39,9 @@ PX_PER_STEP = 2 * W * H  # Sobel pixels + gray pixels
 SOBEL_BYTES = 2 * W * H  # u8 in + u8 out (sum / max fused: 0 extra)
 GRAY_BYTES = 5 * W * H  # uchar4 in + u8 out
 NSETS = 16
+# DRAM bytes (read + write) per launch from one ncu capture of each kernel on
+# this workload (profiles/ holds the summary and the command)
+NCU_TRAFFIC = {}
 METRIC = "Gpixels/s (Sobel3x3 MIRROR + u64 sum + u8 max, and RGBA->gray, 4096x4096)"
 
 
@@ -49,6 +53,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-extras", action="store_true", help="skip the other workloads' kernel timings")
+    ap.add_argument("--only", default=None, choices=list(OTHER_SECTIONS),
+                    help="time one of the other workloads alone (a short run, e.g. for a profiler) and exit")
     return ap.parse_args()
 
 
@@ -186,8 +192,9 @@ def run_reference(args):
                          "sample": f"{steps} full steps of the 4096x4096 pipeline (reference CPU back end restated,"
                                    f" OpenMP over rows)"},
         "e2e": {"value": v, "unit": "Gpixels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "reference CPU back end restated in C++/OpenMP (the reference compiler needs Clang 10 and its CUDA"
-                " runtime does not build on CUDA 13)",
+        "note": "reference CPU back end restated in C++/OpenMP: the reference is not a Python package (pip install"
+                " finds no setup.py or pyproject.toml), its compiler needs Clang 10 and its CUDA runtime does not"
+                " build on CUDA 13",
     }))
 
 
@@ -277,7 +284,7 @@ def run_gb300(args):
         dist.barrier()
     # per-kernel average launch duration, same stream, same rotation
     kern = {}
-    for name, gr, nbytes in (("sobel3_kernel+reduce", g_sobel, SOBEL_BYTES), ("gray_kernel", g_gray, GRAY_BYTES)):
+    for name, gr, nbytes in (("sobel3_tma_kernel", g_sobel, SOBEL_BYTES), ("gray_kernel", g_gray, GRAY_BYTES)):
         reps = max(4, args.steps // NSETS // 2)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(s):
@@ -313,7 +320,8 @@ def run_gb300(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     others = measure_other_configs(dev, peak) if (rank == 0 and not args.no_extras) else None
-    dom = kern["gray_kernel"]
+    dom_name = max(kern, key=lambda k: kern[k]["us_per_launch"])  # the kernel with the larger share of the step
+    dom = kern[dom_name]
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "Gpixels/s", "n_gpus": world, "steps": args.steps,
@@ -326,7 +334,7 @@ def run_gb300(args):
                                                      f"{NSETS * 117} MB)", "launch": "CUDA graph replay",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                         "frac": dom["achieved_gbs"] / peak, "traffic": None, "kernel": "gray_kernel",
+                         "frac": dom["achieved_gbs"] / peak, "traffic": NCU_TRAFFIC.get(dom_name), "kernel": dom_name,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},
             "kernels": kern,
             "other_configs": others,
@@ -386,14 +394,39 @@ def gauss_taps(k, sigma):
     return (g / g.sum()).astype(np.float32)
 
 
-def measure_other_configs(dev, peak_gbs):
-    """Device throughput of the other workloads (graph-replayed, inputs larger than L2)."""
+OTHER_SECTIONS = ("gaussian", "precision", "pyramid", "diff")
+
+
+def measure_other_configs(dev, peak_gbs, only=None):
+    """Device throughput of the other workloads (graph-replayed, inputs larger than L2).
+    `only` restricts the run to one section with the fewest replays."""
     import torch
 
     from hipacc_gb300 import api
 
     s = torch.cuda.Stream(device=dev)
     res = {}
+    q = 1 if only else 0  # replays shrink to one in a single-section run
+
+    def want(sec):
+        return only is None or only == sec
+
+    if want("gaussian"):
+        _gaussian(dev, peak_gbs, s, res, q)
+    if want("precision"):
+        _precision(dev, peak_gbs, s, res, q)
+    if want("pyramid"):
+        _pyramid(dev, peak_gbs, s, res, q)
+    if want("diff"):
+        _diff(dev, s, res, q)
+    return res
+
+
+def _gaussian(dev, peak_gbs, s, res, q):
+    import torch
+
+    from hipacc_gb300 import api
+
     # 5x5 sigma=1 Gaussian, FP32 1024x1024, CLAMP: batches of 64 distinct images per launch
     ax = np.arange(-2, 3, dtype=np.float64)
     m5 = np.exp(-(ax[None, :] ** 2 + ax[:, None] ** 2) / 2.0)
@@ -402,11 +435,18 @@ def measure_other_configs(dev, peak_gbs):
     ins = [torch.rand((64, 1024, 1024), device=dev) for _ in range(nb)]
     outs = [torch.empty_like(x) for x in ins]
     us = graph_time_us(lambda i: api.local_op(ins[i % nb], outs[i % nb], mask=m5, boundary=api.CLAMP, stream=s), nb,
-                       s, 10)
+                       s, 1 if q else 10)
     px = 64 * 1024 * 1024
     res["gaussian5x5_f32_1024_clamp_b64"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
                                              "achieved_gbs": 8 * px / us / 1e3, "frac_hbm": 8 * px / us / 1e3 / peak_gbs}
     del ins, outs
+
+
+def _precision(dev, peak_gbs, s, res, q):
+    import torch
+
+    from hipacc_gb300 import api
+
     # precision: separable 9x9 sigma=2 and 13x13 bilateral on 8192x8192, REPEAT
     img32 = [field(8192, 8192, 20 + i, dev) for i in range(2)]
     taps = gauss_taps(9, 2.0)
@@ -418,7 +458,7 @@ def measure_other_configs(dev, peak_gbs):
         outs = [torch.empty_like(x) for x in ins]
         es = ins[0].element_size()
         us = graph_time_us(lambda i: api.separable(ins[i % 2], outs[i % 2], taps, taps, boundary=api.REPEAT,
-                                                   stream=s), 2, s, 10)
+                                                   stream=s), 2, s, 1 if q else 10)
         res[f"separable9_{name}_8192_repeat"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
                                                  "achieved_gbs": 2 * es * px / us / 1e3,
                                                  "frac_hbm": 2 * es * px / us / 1e3 / peak_gbs}
@@ -433,6 +473,13 @@ def measure_other_configs(dev, peak_gbs):
                                                                   "exp_per_s": 169 * px / us * 1e6}
         del ins, outs
     del img32
+
+
+def _pyramid(dev, peak_gbs, s, res, q):
+    import torch
+
+    from hipacc_gb300 import api
+
     # batching: 64 FP32 images, w and h uniform in [257, 4096], 8-level Laplacian pyramid, MIRROR
     rng = np.random.default_rng(4096)
     ws_ = rng.integers(257, 4097, 64)
@@ -450,10 +497,17 @@ def measure_other_configs(dev, peak_gbs):
             alg += 8.0 * w * h + 4.0 * (w // 2) * (h // 2)  # read G_l, write L_l, write G_{l+1}
             w, h = w // 2, h // 2
     for mode, name in ((0, "persistent_1launch"), (1, "per_level_7launches"), (2, "per_image_per_level_1344launches")):
-        us = graph_time_us(lambda i: plan.decompose(mode, stream=s), 1, s, 3 if mode < 2 else 2)
+        us = graph_time_us(lambda i: plan.decompose(mode, stream=s), 1, s, 1 if q else (3 if mode < 2 else 2))
         res[f"pyramid8_64img_{name}"] = {"us_per_batch": us, "gpix_s": base_px / us / 1e3,
                                          "achieved_gbs": alg / us / 1e3, "frac_hbm": alg / us / 1e3 / peak_gbs}
     plan.close()
+
+
+def _diff(dev, s, res, q):
+    import torch
+
+    from hipacc_gb300 import api
+
     # differentiation: 16 x 2048^2, learnable 7x7 mask + 9x9 bilateral (sigma_d = 2) with learnable sigma_r
     g = torch.Generator(device=dev)
     g.manual_seed(5)
@@ -470,10 +524,9 @@ def measure_other_configs(dev, peak_gbs):
     px = 16 * 2048 * 2048
     for mode, name in ((0, "fused_3launches"), (1, "unfused_per_image")):
         us = graph_time_us(lambda i: api.conv_bilateral_mse(x, t, mask, sigma, sm9, api.CLAMP, mode, stream=s), 1, s,
-                           3)
+                           1 if q else 3)
         res[f"conv7_bilateral9_mse_fwd_adj_16x2048_{name}"] = {"us_per_batch": us, "gpix_s": px / us / 1e3}
     del x, t
-    return res
 
 
 def run_e2e(args, L, dev, rank):
@@ -529,9 +582,25 @@ def run_e2e(args, L, dev, rank):
             "d2h": W * H * 2 + 16}
 
 
+def run_only(args):
+    import torch
+
+    from hipacc_gb300 import api
+
+    api.init(0)
+    dev = torch.device("cuda", 0)
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        peak = 6800.0
+    print(json.dumps({"only": args.only, "timings": measure_other_configs(dev, peak, only=args.only)}))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.only:
+        run_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

@@ -220,8 +220,9 @@ HGB_API int hgb_resample(const hgb_view *in, const hgb_view *out, int imode, voi
  * last-block combine behind a release/acquire ticket.  Result types:
  *   u8/u16/u32 SUM -> uint64, MIN/MAX -> same width as input (stored in a u32/u64 slot)
  *   i16/i32 SUM -> int64;  u64 SUM -> uint64
- *   f32 SUM -> per-thread Kahan partials, FP64 cross-block combine; result_dev
- *   receives a double (the float result is its rounding);  f32 MIN/MAX/PROD -> float
+ *   f32/f16/bf16 SUM -> per-thread Kahan partials, FP64 cross-block combine;
+ *   the 8-byte result is a double (the float result is its rounding)
+ *   f32/f16/bf16 MIN/MAX/PROD -> folded in float, delivered widened to a double
  *   f64 -> double
  * `result_dev` (device, 8 bytes) and/or `result_host` (8 bytes; the call then
  * synchronises the stream). */
