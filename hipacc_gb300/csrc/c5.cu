@@ -69,8 +69,39 @@ struct C5Params {
   int fuse_loss;           // forward writes a (else writes y and W into a)
   int symmetric;           // bilateral adjoint reuses weights
   int fuse_dmask;          // conv adjoint accumulates dL/dmask
-  int img_offset;          // image index of blockIdx.z == 0 (per-image launches)
+  int img_offset;          // image of the launch (per-image launches; 0 otherwise)
+  int tiles_x, tiles_y, ntiles;  // tile grid of the launch (all images, or one image)
+  int combine;             // the launch covers the batch: its last CTA publishes the sums
 };
+
+// tile t of the launch: image, origin
+__device__ __forceinline__ void tile_origin(const C5Params &p, int t, int &b, int &X0, int &Y0) {
+  const int per = p.tiles_x * p.tiles_y;
+  const int bz = t / per, r = t - bz * per;
+  const int by = r / p.tiles_x;
+  b = bz + p.img_offset;
+  X0 = (r - by * p.tiles_x) * C5_TW;
+  Y0 = by * C5_TH;
+}
+
+// Deterministic block-wide FP64 sum of item(0..n-1): thread t folds items
+// t, t + C5_T, ... in order, then a fixed tree over the threads.  Every thread
+// of the block calls it; every thread gets the sum.
+template <class F>
+__device__ __forceinline__ double block_sum_fixed(int n, F item, double *sh) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += C5_T) s += item(i);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+#pragma unroll
+  for (int d = C5_T / 2; d > 0; d >>= 1) {
+    if (threadIdx.x < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
 
 __device__ __forceinline__ float ex2f(float x) {
   float y;
@@ -104,12 +135,18 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
   __shared__ float xs[XS_W * XS_H];
   __shared__ float ys[YS_W * YS_H];
   __shared__ float msk[C5_MK * C5_MK];
-  __shared__ float sbuf[32];
-  const int b = blockIdx.z + p.img_offset;
-  const int X0 = blockIdx.x * C5_TW, Y0 = blockIdx.y * C5_TH;
-  const float *x = p.x + (int64_t)b * p.xb;
+  __shared__ double dsh[C5_T];
   const int W = p.w, H = p.h, bm = p.bmode;
   for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) msk[i] = __ldg(p.mask_dev + i);
+  float c, k2;
+  sigma_consts(p, c, k2);
+  Kahan lsum{0.0f, 0.0f};
+  // persistent: the CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+  int b, X0, Y0;
+  tile_origin(p, tile, b, X0, Y0);
+  const float *x = p.x + (int64_t)b * p.xb;
+  __syncthreads();  // the previous tile's reads of xs / ys are done
   if (p.fuse_conv) {
     constexpr int R = C5_MR + C5_BR;
     for (int c = threadIdx.x; c < XS_W * XS_H; c += C5_T) {
@@ -144,9 +181,6 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
     }
   }
   __syncthreads();
-  float c, k2;
-  sigma_consts(p, c, k2);
-  Kahan lsum{0.0f, 0.0f};
   const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
   for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
     const int gx = X0 + tx, gy = Y0 + py;
@@ -177,8 +211,9 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
       p.a[o] = Wt;  // the unfused chain keeps W and forms a in its own pass
     }
   }
+  }  // tiles
   if (!p.fuse_loss) return;
-  // per-block Kahan partial of the squared error, FP64 combine by the last block
+  // per-CTA Kahan partial of the squared error, FP64 combine by the last CTA
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) {
     Kahan o;
@@ -196,12 +231,14 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
     p.loss_part[block_rank()] = make_float2(k.s, k.c);
   }
   if (take_last_ticket(p.tickets + 0)) {
+    const double s = block_sum_fixed(
+        (int)nb,
+        [&](int i) {
+          const float2 v = __ldcg(p.loss_part + i);
+          return (double)v.x - (double)v.y;
+        },
+        dsh);
     if (threadIdx.x == 0) {
-      double s = 0.0;
-      for (unsigned int i = 0; i < nb; ++i) {
-        const float2 v = __ldcg(p.loss_part + i);
-        s += (double)v.x - (double)v.y;
-      }
       *p.loss_dev = s * p.inv_n;
       p.tickets[0] = 0u;
     }
@@ -243,10 +280,17 @@ __device__ __forceinline__ int preimages(int mode, int j, int n, int rad, int *o
 __global__ void __launch_bounds__(C5_T) c5_bilateral_adjoint_kernel(const __grid_constant__ C5Params p) {
   __shared__ float sa[YS_W * YS_H], sy[YS_W * YS_H], s1[YS_W * YS_H];
   __shared__ float sbuf[32];
-  const int b = blockIdx.z + p.img_offset;
-  const int X0 = blockIdx.x * C5_TW, Y0 = blockIdx.y * C5_TH;
+  __shared__ double dsh[C5_T];
   const int W = p.w, H = p.h, bm = p.bmode;
+  float c, k2;
+  sigma_consts(p, c, k2);
+  const float c2 = 2.0f * c;
+  float dc = 0.0f;
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+  int b, X0, Y0;
+  tile_origin(p, tile, b, X0, Y0);
   const int64_t base = (int64_t)b * p.ib;
+  __syncthreads();  // the previous tile's reads are done
   // in-image cells of [X0-4, X0+TW+4) x [Y0-4, Y0+TH+4); others are never read
   for (int c = threadIdx.x; c < YS_W * YS_H; c += C5_T) {
     const int r = c / YS_W, q = c - r * YS_W;
@@ -259,10 +303,6 @@ __global__ void __launch_bounds__(C5_T) c5_bilateral_adjoint_kernel(const __grid
     }
   }
   __syncthreads();
-  float c, k2;
-  sigma_consts(p, c, k2);
-  const float c2 = 2.0f * c;
-  float dc = 0.0f;
   const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
   auto S = [&](const float *arr, int gy, int gx) { return arr[(gy - Y0 + C5_BR) * YS_W + gx - X0 + C5_BR]; };
   for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
@@ -315,14 +355,14 @@ __global__ void __launch_bounds__(C5_T) c5_bilateral_adjoint_kernel(const __grid
     }
     p.dy1[base + (int64_t)jy * p.ip + jx] = __fmaf_rn(aj, ctr, dn);
   }
+  }  // tiles
   const float bdc = block_sum_f(dc, sbuf);
   const unsigned int nb = grid_blocks();
   const unsigned int rank = block_rank() + (unsigned)p.img_offset * nb;
   if (threadIdx.x == 0) p.dc_part[rank] = bdc;
-  if (p.img_offset == 0 && p.batch > 0 && gridDim.z == (unsigned)p.batch) {
-    if (take_last_ticket(p.tickets + 1) && threadIdx.x == 0) {
-      double s = 0.0;
-      for (unsigned int i = 0; i < nb; ++i) s += (double)__ldcg(p.dc_part + i);
+  if (p.combine && take_last_ticket(p.tickets + 1)) {
+    const double s = block_sum_fixed((int)nb, [&](int i) { return (double)__ldcg(p.dc_part + i); }, dsh);
+    if (threadIdx.x == 0) {
       const double sg = (double)__ldg(p.sigma_dev);
       *p.grad_sigma_dev = (float)(s * (-1.0 / (sg * sg * sg)));
       p.tickets[1] = 0u;
@@ -335,12 +375,18 @@ __global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_cons
   __shared__ float sd[DS_W * DS_H], sx[DS_W * DS_H];
   __shared__ float msk[C5_MK * C5_MK];
   __shared__ float red[C5_T / 32][C5_MK * C5_MK];
-  const int b = blockIdx.z + p.img_offset;
-  const int X0 = blockIdx.x * C5_TW, Y0 = blockIdx.y * C5_TH;
+  __shared__ double dsh[C5_T];
   const int W = p.w, H = p.h, bm = p.bmode;
+  for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) msk[i] = __ldg(p.mask_dev + i);
+  float dm[C5_MK * C5_MK];
+#pragma unroll
+  for (int i = 0; i < C5_MK * C5_MK; ++i) dm[i] = 0.0f;
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+  int b, X0, Y0;
+  tile_origin(p, tile, b, X0, Y0);
   const int64_t base = (int64_t)b * p.ib;
   const float *x = p.x + (int64_t)b * p.xb;
-  for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) msk[i] = __ldg(p.mask_dev + i);
+  __syncthreads();  // the previous tile's reads are done
   for (int c = threadIdx.x; c < DS_W * DS_H; c += C5_T) {
     const int r = c / DS_W, q = c - r * DS_W;
     const int gy = Y0 - C5_MR + r, gx = X0 - C5_MR + q;
@@ -350,9 +396,6 @@ __global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_cons
   }
   __syncthreads();
   auto D = [&](int gy, int gx) { return sd[(gy - Y0 + C5_MR) * DS_W + gx - X0 + C5_MR]; };
-  float dm[C5_MK * C5_MK];
-#pragma unroll
-  for (int i = 0; i < C5_MK * C5_MK; ++i) dm[i] = 0.0f;
   const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
   for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
     const int ix = X0 + tx, iy = Y0 + py;
@@ -390,6 +433,7 @@ __global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_cons
         }
     }
   }
+  }  // tiles
   if (!p.fuse_dmask) return;
   // block partials of dL/dmask (49 values), FP64 combine by the last block
 #pragma unroll
@@ -406,16 +450,15 @@ __global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_cons
     float s = 0.0f;
     for (int wv = 0; wv < C5_T / 32; ++wv) s += red[wv][threadIdx.x];
     p.dm_part[(size_t)rank * C5_MK * C5_MK + threadIdx.x] = s;
+    __threadfence();
   }
-  if (p.img_offset == 0 && gridDim.z == (unsigned)p.batch) {
-    if (take_last_ticket(p.tickets + 2)) {
-      if (threadIdx.x < C5_MK * C5_MK) {
-        double s = 0.0;
-        for (unsigned int i = 0; i < nb; ++i) s += (double)__ldcg(p.dm_part + (size_t)i * C5_MK * C5_MK + threadIdx.x);
-        p.grad_mask_dev[threadIdx.x] = (float)s;
-      }
-      if (threadIdx.x == 0) p.tickets[2] = 0u;
+  if (p.combine && take_last_ticket(p.tickets + 2)) {
+    for (int o = 0; o < C5_MK * C5_MK; ++o) {
+      const double s = block_sum_fixed(
+          (int)nb, [&](int i) { return (double)__ldcg(p.dm_part + (size_t)i * C5_MK * C5_MK + o); }, dsh);
+      if (threadIdx.x == 0) p.grad_mask_dev[o] = (float)s;
     }
+    if (threadIdx.x == 0) p.tickets[2] = 0u;
   }
 }
 
@@ -438,24 +481,22 @@ __global__ void __launch_bounds__(C5_T) c5_dmask_kernel(const __grid_constant__ 
   if (threadIdx.x == 0) p.dm_part[((size_t)p.img_offset * gridDim.y + blockIdx.y) * C5_MK * C5_MK + o] = v;
 }
 
-// unfused chain: final FP64 combines of the per-image partials
-__global__ void c5_combine_kernel(const __grid_constant__ C5Params p, int loss_parts, int dc_parts, int dm_parts) {
-  const int i = threadIdx.x;
-  if (i < C5_MK * C5_MK) {
-    double s = 0.0;
-    for (int k = 0; k < dm_parts; ++k) s += (double)p.dm_part[(size_t)k * C5_MK * C5_MK + i];
-    p.grad_mask_dev[i] = (float)s;
+// unfused chain: final FP64 combines of the per-image partials (one CTA,
+// fixed order)
+__global__ void __launch_bounds__(C5_T) c5_combine_kernel(const __grid_constant__ C5Params p, int loss_parts,
+                                                          int dc_parts, int dm_parts) {
+  __shared__ double dsh[C5_T];
+  for (int o = 0; o < C5_MK * C5_MK; ++o) {
+    const double s =
+        block_sum_fixed(dm_parts, [&](int k) { return (double)p.dm_part[(size_t)k * C5_MK * C5_MK + o]; }, dsh);
+    if (threadIdx.x == 0) p.grad_mask_dev[o] = (float)s;
   }
-  if (i == 64) {
-    double s = 0.0;
-    for (int k = 0; k < loss_parts; ++k) s += (double)p.loss_part[k].x;
-    *p.loss_dev = s * p.inv_n;
-  }
-  if (i == 96) {
-    double s = 0.0;
-    for (int k = 0; k < dc_parts; ++k) s += (double)p.dc_part[k];
+  const double l = block_sum_fixed(loss_parts, [&](int k) { return (double)p.loss_part[k].x; }, dsh);
+  const double dc = block_sum_fixed(dc_parts, [&](int k) { return (double)p.dc_part[k]; }, dsh);
+  if (threadIdx.x == 0) {
+    *p.loss_dev = l * p.inv_n;
     const double sg = (double)p.sigma_dev[0];
-    *p.grad_sigma_dev = (float)(s * (-1.0 / (sg * sg * sg)));
+    *p.grad_sigma_dev = (float)(dc * (-1.0 / (sg * sg * sg)));
   }
 }
 
@@ -542,20 +583,36 @@ extern "C" int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, cons
   p.loss_dev = loss_dev;
   p.grad_mask_dev = grad_mask_dev;
   p.grad_sigma_dev = grad_sigma_dev;
+  p.tiles_x = (int)grid.x;
+  p.tiles_y = (int)grid.y;
   cudaStream_t st = (cudaStream_t)stream;
+  // persistent grids: one wave of resident CTAs walking the tiles
+  static int occ[3] = {0, 0, 0};
+  if (!occ[0]) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], c5_forward_kernel, C5_T, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], c5_bilateral_adjoint_kernel, C5_T, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], c5_conv_adjoint_kernel, C5_T, 0) != cudaSuccess)
+      occ[0] = occ[1] = occ[2] = 1;
+    for (int i = 0; i < 3; ++i) occ[i] = std::max(occ[i], 1);
+  }
+  auto wave = [&](int k, int ntiles) { return std::max(1, std::min(ntiles, num_sms() * occ[k])); };
   cudaEvent_t ev = before_launch(st);
   if (mode == 0) {
     p.fuse_conv = 1;
     p.fuse_loss = 1;
     p.symmetric = 1;
     p.fuse_dmask = 1;
-    c5_forward_kernel<<<grid, C5_T, 0, st>>>(p);
-    c5_bilateral_adjoint_kernel<<<grid, C5_T, 0, st>>>(p);
-    c5_conv_adjoint_kernel<<<grid, C5_T, 0, st>>>(p);
+    p.combine = 1;
+    p.ntiles = (int)nblk;
+    c5_forward_kernel<<<wave(0, p.ntiles), C5_T, 0, st>>>(p);
+    c5_bilateral_adjoint_kernel<<<wave(1, p.ntiles), C5_T, 0, st>>>(p);
+    c5_conv_adjoint_kernel<<<wave(2, p.ntiles), C5_T, 0, st>>>(p);
     return after_launch("c5 fused", st, ev);
   }
   // unfused chain, one image at a time
   const dim3 g1(grid.x, grid.y, 1);
+  const int per_image = (int)(grid.x * grid.y);
+  const int g_bil = wave(1, per_image);
   for (int b = 0; b < B; ++b) {
     hgb_view xv{(void *)(p.x + (int64_t)b * p.xb), HGB_F32, W, H, 1, x->pitch, x->pitch * H};
     hgb_view yv{p.y1 + (int64_t)b * ib, HGB_F32, W, H, 1, ip * 4, ib * 4};
@@ -568,12 +625,14 @@ extern "C" int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, cons
     q.fuse_loss = 0;
     q.symmetric = 0;
     q.fuse_dmask = 0;
-    c5_forward_kernel<<<g1, C5_T, 0, st>>>(q);
+    q.combine = 0;
+    q.ntiles = per_image;
+    c5_forward_kernel<<<wave(0, per_image), C5_T, 0, st>>>(q);
     c5_alpha_kernel<<<g1, C5_T, 0, st>>>(q);
-    c5_bilateral_adjoint_kernel<<<g1, C5_T, 0, st>>>(q);
-    c5_conv_adjoint_kernel<<<g1, C5_T, 0, st>>>(q);
+    c5_bilateral_adjoint_kernel<<<g_bil, C5_T, 0, st>>>(q);
+    c5_conv_adjoint_kernel<<<wave(2, per_image), C5_T, 0, st>>>(q);
     c5_dmask_kernel<<<dim3(C5_MK * C5_MK, red_rows, 1), C5_T, 0, st>>>(q);
   }
-  c5_combine_kernel<<<1, 128, 0, st>>>(p, (int)nblk, (int)nblk, B * red_rows);
+  c5_combine_kernel<<<1, C5_T, 0, st>>>(p, (int)nblk, B * g_bil, B * red_rows);
   return after_launch("c5 unfused", st, ev);
 }

@@ -16,6 +16,8 @@
 // D = bottom - top.  Other masks: sobel_generic_kernel.  Every path reduces
 // sum and max with redux.sync across the warp, shared memory across the block
 // and a last-block combine of the per-block partials.
+#include <algorithm>
+
 #include "reduce_common.cuh"
 #include "tma.cuh"
 
@@ -206,29 +208,34 @@ __global__ void __launch_bounds__(SB_BX *SB_BY) sobel3_kernel(const __grid_const
 
 
 // ---------------------------------------------------------------------------
-// TMA path for the standard 3x3 masks.  Persistent CTAs each own a contiguous
-// range of 128 x 32 output tiles (about SMs x 8 CTAs, equal tile counts).  The
-// 160 x 34 byte halo tile of each is loaded by cp.async.bulk.tensor into a
-// 4-stage ring, so a CTA has up to four tiles in flight from its first cycle.
-// Cells outside the image (TMA fills them with 0) are patched with the
-// boundary rule before use.  Arithmetic is fp16x2 on exact integers: every
-// intermediate (|gx|, |gy| <= 1020, their sum <= 2040) is an integer below
-// 2048 and therefore exact in half precision, so results are the integer
-// results bit for bit.  Bytes become halves by placing them under the
-// exponent byte 0x64 (1024 + v) with one byte permute per pair.
+// TMA path for the standard 3x3 masks.  Work unit: a 128 x 16 output tile,
+// staged as its 160 x 18 byte halo tile by one cp.async.bulk.tensor load.
+// Every warp runs its own two-stage pipeline (own shared-memory ring, own
+// mbarriers, no block-wide barrier): its lane 0 claims the next tile, issues
+// the load and the whole warp waits on that stage only.  CTA c owns tiles
+// c, c + G, c + 2G, ... (G CTAs, two per SM) and its 16 warps claim them from
+// a shared-memory counter, so SMs get equal shares and warps balance inside
+// the CTA.  Cells outside the image (TMA fills them with 0) are patched with
+// the boundary rule by the owning warp before use.
+//
+// Arithmetic is fp16x2 on exact integers: every intermediate (|gx|, |gy| <=
+// 1020, their sum <= 2040) is an integer below 2048 and therefore exact in
+// half precision, so results are the integer results bit for bit.  Bytes
+// become halves by placing them under the exponent byte 0x64 (1024 + v) with
+// one byte permute per pair.
 struct SobelTmaParams {
   CUtensorMap map;
   SobelParams p;
-  int tiles_x, tiles_y, ntiles, tiles_per_cta;
+  int tiles_x, tiles_y, ntiles;
   int *status;
   unsigned long long *acc;  // workspace accumulators (sum, max), zero at rest
   unsigned int *ticket;
 };
 
-constexpr int T_TW = 128, T_TH = 32, T_BX = 32, T_BY = 4, T_PY = 8;
+constexpr int T_TW = 128, T_TH = 16, T_WARPS = 16, T_NST = 2, T_CPS = 2;
 constexpr int T_SW = 160, T_SH = T_TH + 2, T_STAGE = T_SW * T_SH;
 constexpr int T_STAGE_PAD = (T_STAGE + 127) / 128 * 128;
-constexpr int T_NST = 4;
+constexpr size_t T_SMEM = (size_t)T_WARPS * T_NST * T_STAGE_PAD + 128;  // + alignment slack
 
 __device__ __forceinline__ __half2 u2h(uint32_t u) {
   __half2 h;
@@ -241,15 +248,15 @@ __device__ __forceinline__ uint32_t h2u(__half2 h) {
   return u;
 }
 
-// One staged tile through the stencil.  FULL: every output of the tile is
-// inside the image and 4-byte stores are legal (no masks, no edge branches).
-// Rows stream through a three-row window of biased pairs P = 1024 + v:
-// row differences H = P(x+1) - P(x-1) and vertical differences
-// V = P(bottom) - P(top) cancel the bias exactly, so
+// One staged tile through the stencil, R output rows per lane.  FULL: every
+// output of the tile is inside the image and 4-byte stores are legal (no
+// masks, no edge branches).  Rows stream through a three-row window of biased
+// pairs P = 1024 + v: row differences H = P(x+1) - P(x-1) and vertical
+// differences V = P(bottom) - P(top) cancel the bias exactly, so
 // gx = H_top + 2 H_mid + H_bottom and gy = V(x-1) + 2 V(x) + V(x+1).
-template <bool FULL>
+template <bool FULL, int R>
 __device__ __forceinline__ void sobel_tile(const SobelParams &p, const uint8_t *tile, uint8_t *out_row, int xo, int yo,
-                                           int xs, int r0, uint32_t &tsum, __half2 &tmax) {
+                                           int xs, uint32_t &tsum, __half2 &tmax) {
   const uint32_t K = 0x64646464u;
   const __half2 c1024 = __float2half2_rn(1024.0f), c255 = __float2half2_rn(255.0f), two = __float2half2_rn(2.0f);
   __half2 P[3][5], H01[3], H23[3];
@@ -259,9 +266,9 @@ __device__ __forceinline__ void sobel_tile(const SobelParams &p, const uint8_t *
     v23 = __halves2half2(__float2half(xo + 2 < p.w ? 1.f : 0.f), __float2half(xo + 3 < p.w ? 1.f : 0.f));
   }
 #pragma unroll
-  for (int r = 0; r < T_PY + 2; ++r) {
+  for (int r = 0; r < R + 2; ++r) {
     const int c = r % 3;
-    const uint8_t *row = tile + (r0 + r) * T_SW + xs;
+    const uint8_t *row = tile + r * T_SW + xs;
     const uint32_t w0 = *reinterpret_cast<const uint32_t *>(row - 4);
     const uint32_t w1 = *reinterpret_cast<const uint32_t *>(row);
     const uint32_t w2 = *reinterpret_cast<const uint32_t *>(row + 4);
@@ -309,14 +316,24 @@ __device__ __forceinline__ void sobel_tile(const SobelParams &p, const uint8_t *
   }
 }
 
-__global__ void __launch_bounds__(T_BX *T_BY, 8) sobel3_tma_kernel(const __grid_constant__ SobelTmaParams P) {
-  __shared__ __align__(128) uint8_t buf[T_NST * T_STAGE_PAD];
-  __shared__ __align__(8) uint64_t bar[T_NST];
-  __shared__ int s_coord[3];
+__global__ void __launch_bounds__(T_WARPS * 32, T_CPS) sobel3_tma_kernel(const __grid_constant__ SobelTmaParams P) {
+  extern __shared__ __align__(128) uint8_t sobel_dsm[];
+  __shared__ __align__(8) uint64_t bar[T_WARPS][T_NST];
+  __shared__ int s_tile[T_WARPS][T_NST];
+  __shared__ int s_next;
+  __shared__ uint32_t s_sum[T_WARPS], s_max[T_WARPS];
   const SobelParams &p = P.p;
-  const int tid = threadIdx.x;
-  const int t0 = blockIdx.x * P.tiles_per_cta;
-  const int nt = min(P.tiles_per_cta, P.ntiles - t0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int G = gridDim.x, c = blockIdx.x;
+  const int n_c = c < P.ntiles ? (P.ntiles - c + G - 1) / G : 0;
+  if (threadIdx.x == 0) s_next = 0;
+  if (lane == 0) {
+    for (int s = 0; s < T_NST; ++s) mbar_init(&bar[warp][s], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  uint8_t *ring = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(sobel_dsm) + 127) & ~(uintptr_t)127) +
+                  warp * T_NST * T_STAGE_PAD;
   auto coords = [&](int t, int &b, int &i0, int &j0) {
     const int tx_ = t % P.tiles_x;
     const int r = t / P.tiles_x;
@@ -324,47 +341,45 @@ __global__ void __launch_bounds__(T_BX *T_BY, 8) sobel3_tma_kernel(const __grid_
     b = r / P.tiles_y;
     i0 = tx_ * T_TW;
   };
-  auto issue = [&](int k) {
-    int b, i0, j0;
-    coords(t0 + k, b, i0, j0);
-    const int st = k % T_NST;
-    fence_proxy_async_smem();
-    mbar_expect_tx(&bar[st], T_STAGE);
-    tma_load_3d(buf + st * T_STAGE_PAD, &P.map, i0 - 16, j0 - 1, b, &bar[st]);
+  // lane 0: claim the CTA's next tile and issue its load into stage st
+  auto claim_issue = [&](int st) {
+    int t = -1;
+    const int k = atomicAdd(&s_next, 1);
+    if (k < n_c) {
+      t = c + k * G;
+      int b, i0, j0;
+      coords(t, b, i0, j0);
+      fence_proxy_async_smem();
+      mbar_expect_tx(&bar[warp][st], T_STAGE);
+      tma_load_3d(ring + st * T_STAGE_PAD, &P.map, i0 - 16, j0 - 1, b, &bar[warp][st]);
+    }
+    s_tile[warp][st] = t;
   };
-  if (tid == 0) {
-    for (int i = 0; i < T_NST; ++i) mbar_init(&bar[i], 1);
-    mbar_fence_init();
-    for (int k = 0; k < T_NST && k < nt; ++k) issue(k);
-  }
-  __syncthreads();
-
-  const int tx = tid % T_BX, ty = tid / T_BX;
-  const int xs = 16 + 4 * tx, r0 = T_PY * ty;
+  if (lane == 0)
+    for (int s = 0; s < T_NST; ++s) claim_issue(s);
+  __syncwarp();
   uint32_t tsum = 0;
   __half2 tmax = __float2half2_rn(0.0f);
-  for (int k = 0; k < nt; ++k) {
-    const int st = k % T_NST;
-    // one thread polls the mbarrier; the others block in the hardware barrier
-    // (its CTA-scope ordering publishes the TMA bytes the poller acquired)
-    int ok = 1;
-    if (tid == 0) {
-      ok = mbar_wait(&bar[st], (k / T_NST) & 1);
-      int b, i0, j0;
-      coords(t0 + k, b, i0, j0);
-      s_coord[0] = b;
-      s_coord[1] = i0;
-      s_coord[2] = j0;
-    }
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) {
+  const int xs = 16 + 4 * lane;
+  for (int it = 0;; ++it) {
+    const int st = it % T_NST;
+    const int t = s_tile[warp][st];
+    if (t < 0) break;
+    const bool ok = mbar_wait(&bar[warp][st], (it / T_NST) & 1);
+    if (!__all_sync(0xffffffffu, ok)) {
+      if (lane == 0) {
         record_status(P.status, HGB_ERR_TIMEOUT);
-        for (int j = k + 1; j < nt && j < k + T_NST; ++j) mbar_wait(&bar[j % T_NST], (j / T_NST) & 1);
+        // the other stage may still have a load in flight: wait for it (bounded)
+        for (int j = 1; j < T_NST; ++j) {
+          const int s2 = (it + j) % T_NST;
+          if (s_tile[warp][s2] >= 0) mbar_wait(&bar[warp][s2], ((it + j) / T_NST) & 1);
+        }
       }
       break;
     }
-    const int b = s_coord[0], i0 = s_coord[1], j0 = s_coord[2];
-    uint8_t *tile = buf + st * T_STAGE_PAD;
+    int b, i0, j0;
+    coords(t, b, i0, j0);
+    uint8_t *tile = ring + st * T_STAGE_PAD;
     const int X0 = i0 - 16, Y0 = j0 - 1;
     if (X0 + 15 < 0 || X0 + 145 > p.w || Y0 < 0 || Y0 + T_SH > p.h) {
       // Patch the staged cells outside the image that the stencil reads
@@ -377,52 +392,52 @@ __global__ void __launch_bounds__(T_BX *T_BY, 8) sobel3_tma_kernel(const __grid_
       const int ntop = max(0, -Y0);
       const int bs = max(0, p.h - Y0), nb = max(0, T_SH - bs);
       const int n1 = nl * T_SH, n2 = n1 + nr * T_SH, n3 = n2 + ntop * ncol, n4 = n3 + nb * ncol;
-      for (int c = tid; c < n4; c += T_BX * T_BY) {
+      for (int cc = lane; cc < n4; cc += 32) {
         int r, q;
-        if (c < n1) {
-          r = c / nl;
-          q = qa + (c - r * nl);
-        } else if (c < n2) {
-          const int d = c - n1;
+        if (cc < n1) {
+          r = cc / nl;
+          q = qa + (cc - r * nl);
+        } else if (cc < n2) {
+          const int d = cc - n1;
           r = d / nr;
           q = rs + (d - r * nr);
-        } else if (c < n3) {
-          const int d = c - n2;
+        } else if (cc < n3) {
+          const int d = cc - n2;
           r = d / ncol;
           q = qa + (d - r * ncol);
         } else {
-          const int d = c - n3;
+          const int d = cc - n3;
           const int rr = d / ncol;
           r = bs + rr;
           q = qa + (d - rr * ncol);
         }
         tile[r * T_SW + q] = (uint8_t)sb_load_px(p, img, X0 + q, Y0 + r);
       }
-      __syncthreads();
+      __syncwarp();
     }
-    const int xo = i0 + 4 * tx, yo = j0 + r0;
-    uint8_t *out_row = p.out + (int64_t)b * p.out_bstride + (int64_t)yo * p.out_pitch + xo;
+    const int xo = i0 + 4 * lane;
+    uint8_t *out_row = p.out + (int64_t)b * p.out_bstride + (int64_t)j0 * p.out_pitch + xo;
     if (p.vec_out && i0 + T_TW <= p.w && j0 + T_TH <= p.h)
-      sobel_tile<true>(p, tile, out_row, xo, yo, xs, r0, tsum, tmax);
+      sobel_tile<true, T_TH>(p, tile, out_row, xo, j0, xs, tsum, tmax);
     else
-      sobel_tile<false>(p, tile, out_row, xo, yo, xs, r0, tsum, tmax);
-    __syncthreads();  // the stage is read; refill it with the tile T_NST ahead
-    if (tid == 0 && k + T_NST < nt) issue(k + T_NST);
+      sobel_tile<false, T_TH>(p, tile, out_row, xo, j0, xs, tsum, tmax);
+    __syncwarp();  // the stage is read; refill it with this warp's next tile
+    if (lane == 0) claim_issue(st);
+    __syncwarp();
   }
   if (p.sum_dev || p.max_dev) {
     const float2 mf = __half22float2(tmax);
-    uint32_t bs = __reduce_add_sync(0xffffffffu, tsum);
-    uint32_t bm = __reduce_max_sync(0xffffffffu, (uint32_t)fmaxf(mf.x, mf.y));
-    __shared__ uint32_t s_sum[T_BX * T_BY / 32], s_max[T_BX * T_BY / 32];
-    if ((tid & 31) == 0) {
-      s_sum[tid >> 5] = bs;
-      s_max[tid >> 5] = bm;
+    const uint32_t bs = __reduce_add_sync(0xffffffffu, tsum);
+    const uint32_t bm = __reduce_max_sync(0xffffffffu, (uint32_t)fmaxf(mf.x, mf.y));
+    if (lane == 0) {
+      s_sum[warp] = bs;
+      s_max[warp] = bm;
     }
     __syncthreads();
-    if (tid == 0) {
+    if (threadIdx.x == 0) {
       unsigned long long S = 0, M = 0;
 #pragma unroll
-      for (int i = 0; i < T_BX * T_BY / 32; ++i) {
+      for (int i = 0; i < T_WARPS; ++i) {
         S += s_sum[i];
         M = M > s_max[i] ? M : s_max[i];
       }
@@ -531,14 +546,17 @@ extern "C" int hgb_sobel_mag(const hgb_view *in, const hgb_view *out, const int 
     rc = make_tensor_map_3d(&P.map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, in->data, p.w, p.h, in->batch, in->pitch,
                             in->batch_stride, T_SW, T_SH);
     if (rc == HGB_OK) {
-      // equal contiguous tile ranges over about one resident wave of CTAs
+      // one resident wave: T_CPS CTAs per SM (fewer if the SM holds fewer)
       static int per_sm = 0;
-      if (!per_sm &&
-          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sobel3_tma_kernel, T_BX * T_BY, 0) != cudaSuccess)
-        per_sm = 4;
-      const int max_ctas = num_sms() * (per_sm > 0 ? per_sm : 4);
-      P.tiles_per_cta = cdiv(P.ntiles, max_ctas);
-      const int g = cdiv(P.ntiles, P.tiles_per_cta);
+      if (!per_sm) {
+        if (cudaFuncSetAttribute(sobel3_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T_SMEM) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sobel3_tma_kernel, T_WARPS * 32, T_SMEM) !=
+                cudaSuccess)
+          return set_error(HGB_ERR_CUDA, "hgb_sobel_mag: kernel attributes");
+        per_sm = std::max(1, std::min(per_sm, T_CPS));
+      }
+      const int g = std::max(1, std::min(P.ntiles, num_sms() * per_sm));
       if (sum_dev || max_dev) {
         Workspace ws;
         rc = workspace_get(0, &ws);
@@ -547,7 +565,7 @@ extern "C" int hgb_sobel_mag(const hgb_view *in, const hgb_view *out, const int 
         P.ticket = ws.tickets + 0;
       }
       cudaEvent_t ev = before_launch(st);
-      sobel3_tma_kernel<<<g, T_BX * T_BY, 0, st>>>(P);
+      sobel3_tma_kernel<<<g, T_WARPS * 32, T_SMEM, st>>>(P);
       return after_launch("sobel3_tma_kernel", st, ev);
     }
   }
