@@ -5,15 +5,18 @@ min(|gx|+|gy|, 255) with Boundary::MIRROR and the fused global u64 sum and u8
 max of the result, plus one 4096x4096 uchar4 image through the RGBA->gray
 point operator (77R + 150G + 29B) >> 8.  Steps rotate over NSETS resident
 image pairs (NSETS x 117 MB, several times the 129 MB L2), so every step reads
-its inputs from HBM.  Steps are replayed from CUDA graphs.
+its inputs from HBM.  Steps are replayed from CUDA graphs; the two operators
+of a step are independent and run as parallel branches of the graph.
 
 Metric: Gpixels/s = (Sobel pixels + gray pixels) per second, whole job.
 `roofline` is for the dominant kernel (the one with the longer launch: Sobel at
 2 algorithmic bytes per pixel or gray at 5); `kernels` lists both kernels'
 achieved HBM bandwidth.
 `e2e` drives the same step through the C ABI with host buffers
-(hgb_image_write / kernels / hgb_image_read): pinned host -> device copies of
-both inputs and device -> host reads of both outputs and the two scalars.
+(hgb_image_write / kernels / hgb_image_read_async): pinned host -> device
+copies of both inputs and device -> host reads of both outputs and the two
+scalars every step, two steps in flight (one uploading while the other reads
+back).
 
 --impl reference times the reference's CPU path for the same step (the
 oracle's restatement of the CPU back end, OpenMP over all host cores).
@@ -230,9 +233,20 @@ def run_gb300(args):
     def gray(i, stream=None):
         api.gray(rgbas[i], grays[i], stream=stream)
 
+    side = torch.cuda.Stream(device=dev)
+
     def step(i, stream=None):
-        sobel(i, stream)
-        gray(i, stream)
+        # the two operators of a step are independent: a fork / join over two
+        # streams makes them parallel branches of the captured graph
+        st = stream if stream is not None else torch.cuda.current_stream()
+        fork = torch.cuda.Event()
+        fork.record(st)
+        side.wait_event(fork)
+        sobel(i, st)
+        gray(i, side)
+        join = torch.cuda.Event()
+        join.record(side)
+        st.wait_event(join)
 
     # eager warm-up + correctness spot check of set 0 against torch arithmetic
     for i in range(NSETS):
@@ -284,7 +298,7 @@ def run_gb300(args):
         dist.barrier()
     # per-kernel average launch duration, same stream, same rotation
     kern = {}
-    for name, gr, nbytes in (("sobel3_tma_kernel", g_sobel, SOBEL_BYTES), ("gray_kernel", g_gray, GRAY_BYTES)):
+    for name, gr, nbytes in (("sobel3_tma_kernel", g_sobel, SOBEL_BYTES), ("gray_bulk_kernel", g_gray, GRAY_BYTES)):
         reps = max(4, args.steps // NSETS // 2)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(s):
@@ -530,7 +544,16 @@ def _diff(dev, s, res, q):
 
 
 def run_e2e(args, L, dev, rank):
-    """Host buffers in, host results out, every step through the C ABI."""
+    """Host buffers in, host results out, every step through the C ABI.
+
+    Each step uploads its two input images from pinned host memory
+    (hgb_image_write), runs the Sobel (+ fused sum / max) and gray kernels and
+    queues the read-back of both output images and both scalars.  Steps
+    alternate between two device image sets on two streams, so one step's
+    read-back and the next step's upload overlap on the link; the kernels of
+    consecutive steps are ordered by an event (they share the library's
+    reduction workspace).  The timed region ends when every read-back landed.
+    """
     import torch
 
     lib = L.load()
@@ -538,46 +561,62 @@ def run_e2e(args, L, dev, rank):
     n_e2e = max(4, min(args.steps // 8, 200))
     h_img = torch.from_numpy(rng.integers(0, 256, (H, W), dtype=np.uint8)).pin_memory()
     h_rgba = torch.from_numpy(rng.integers(0, 256, (H, W, 4), dtype=np.uint8)).pin_memory()
-    h_mag = torch.empty((H, W), dtype=torch.uint8).pin_memory()
-    h_gray = torch.empty((H, W), dtype=torch.uint8).pin_memory()
-    h_scalars = torch.empty(4, dtype=torch.int64).pin_memory()
-    imgs = {}
-    for name, dt in (("img", L.U8), ("rgba", L.U8X4), ("mag", L.U8), ("gray", L.U8)):
-        p = C.c_void_p()
-        L.check(lib.hgb_image_create(dt, W, H, 256, None, C.byref(p)))
-        imgs[name] = p
-    views = {}
-    for k, p in imgs.items():
-        v = L.View()
-        L.check(lib.hgb_image_get_view(p, C.byref(v)))
-        views[k] = v
-    scal = torch.zeros(2, dtype=torch.int64, device=dev)
-    st = torch.cuda.current_stream()
-    sp = C.c_void_p(st.cuda_stream)
+    nset = 2
+    h_mag = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(nset)]
+    h_gray = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(nset)]
+    h_scalars = [torch.empty(2, dtype=torch.int64).pin_memory() for _ in range(nset)]
+    sets = []
+    for _ in range(nset):
+        imgs, views = {}, {}
+        for name, dt in (("img", L.U8), ("rgba", L.U8X4), ("mag", L.U8), ("gray", L.U8)):
+            p = C.c_void_p()
+            L.check(lib.hgb_image_create(dt, W, H, 256, None, C.byref(p)))
+            v = L.View()
+            L.check(lib.hgb_image_get_view(p, C.byref(v)))
+            imgs[name], views[name] = p, v
+        sets.append((imgs, views, torch.zeros(2, dtype=torch.int64, device=dev)))
+    streams = [torch.cuda.Stream(device=dev) for _ in range(nset)]
+    done = [torch.cuda.Event() for _ in range(nset)]
     mx = np.array([-1, 0, 1, -2, 0, 2, -1, 0, 1], np.int32)
     my = np.array([-1, -2, -1, 0, 0, 0, 1, 2, 1], np.int32)
 
-    def one():
+    def one(k):
+        j = k % nset
+        imgs, views, scal = sets[j]
+        st = streams[j]
+        sp = C.c_void_p(st.cuda_stream)
         L.check(lib.hgb_image_write(imgs["img"], C.c_void_p(h_img.data_ptr()), sp))
         L.check(lib.hgb_image_write(imgs["rgba"], C.c_void_p(h_rgba.data_ptr()), sp))
+        if k > 0:
+            st.wait_event(done[(k - 1) % nset])  # kernels in step order
         L.check(lib.hgb_sobel_mag(C.byref(views["img"]), C.byref(views["mag"]), mx.ctypes.data_as(C.c_void_p),
                                   my.ctypes.data_as(C.c_void_p), 3, L.MIRROR, 0, C.c_void_p(scal.data_ptr()),
                                   C.c_void_p(scal.data_ptr() + 8), sp))
         L.check(lib.hgb_point_gray(C.byref(views["rgba"]), C.byref(views["gray"]), 77, 150, 29, 8, sp))
-        L.check(lib.hgb_image_read(imgs["mag"], C.c_void_p(h_mag.data_ptr()), sp))
-        L.check(lib.hgb_image_read(imgs["gray"], C.c_void_p(h_gray.data_ptr()), sp))
-        h_scalars[:2].copy_(scal, non_blocking=False)
+        done[j].record(st)
+        L.check(lib.hgb_image_read_async(imgs["mag"], C.c_void_p(h_mag[j].data_ptr()), sp))
+        L.check(lib.hgb_image_read_async(imgs["gray"], C.c_void_p(h_gray[j].data_ptr()), sp))
+        with torch.cuda.stream(st):
+            h_scalars[j].copy_(scal, non_blocking=True)
 
-    for _ in range(3):
-        one()
+    for k in range(4):
+        one(k)
     torch.cuda.synchronize()
+    # the warm-up read-backs must be right: gray against numpy, the fused sum / max against the read-back image
+    rgba = h_rgba.numpy().astype(np.uint32)
+    ref_gray = ((77 * rgba[..., 0] + 150 * rgba[..., 1] + 29 * rgba[..., 2]) >> 8).astype(np.uint8)
+    mag = h_mag[1].numpy()
+    if not (np.array_equal(h_gray[1].numpy(), ref_gray) and int(h_scalars[1][0]) == int(mag.sum(dtype=np.uint64))
+            and int(h_scalars[1][1]) == int(mag.max())):
+        raise RuntimeError("end-to-end read-back does not match")
     t0 = time.perf_counter()
-    for _ in range(n_e2e):
-        one()
+    for k in range(n_e2e):
+        one(k)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
-    for p in imgs.values():
-        lib.hgb_image_destroy(p)
+    for imgs, _, _ in sets:
+        for p in imgs.values():
+            lib.hgb_image_destroy(p)
     return {"elapsed": el, "pixels": n_e2e * PX_PER_STEP, "steps": n_e2e, "h2d": W * H * 5,
             "d2h": W * H * 2 + 16}
 

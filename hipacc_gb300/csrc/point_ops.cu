@@ -6,7 +6,9 @@
 // from include/hipacc/Device/TargetDescription.h:85-91).  Here every thread
 // moves 16 pixels with 16-byte vector loads and stores over a grid sized to
 // the SM count; dense images are treated as one long row.
-#include "hgb_internal.cuh"
+#include <algorithm>
+
+#include "tma.cuh"
 
 namespace hgb {
 namespace {
@@ -237,6 +239,63 @@ __global__ void __launch_bounds__(256) resample_kernel(const char *in, int64_t i
   }
 }
 
+// ---------------------------------------------------------------- gray, bulk copies
+// Dense images (rows back to back, the batch contiguous) are one flat array of
+// N pixels, cut into units of GB_UNIT pixels (16 KiB of uchar4).  Each CTA
+// takes one unit: thread 0 issues one cp.async.bulk of the unit into shared
+// memory (completion on an mbarrier) and every thread turns 16 staged pixels
+// into one 16-byte store.  With 16 KiB of shared memory per CTA the SM holds
+// up to 8 such CTAs, so many copies are in flight without a software pipeline,
+// and an independent kernel of the same step can share the SMs.  The last CTA
+// converts the pixels after the last whole unit with plain loads.
+constexpr int GB_T = 256, GB_UNIT = 16 * GB_T;
+constexpr int GB_STAGE = GB_UNIT * 4;
+
+struct GrayBulkParams {
+  GrayParams p;
+  int64_t npx;  // pixels of the flat array
+  int64_t nunits;
+  int *status;
+};
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__global__ void __launch_bounds__(GB_T) gray_bulk_kernel(const __grid_constant__ GrayBulkParams B) {
+  __shared__ __align__(128) uint8_t stage[GB_STAGE];
+  __shared__ __align__(8) uint64_t bar;
+  const GrayParams &p = B.p;
+  const int64_t u = blockIdx.x;
+  if (u < B.nunits) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bar, 1);
+      mbar_fence_init();
+      mbar_expect_tx(&bar, GB_STAGE);
+      bulk_load(stage, p.in + u * GB_STAGE, GB_STAGE, &bar);
+    }
+    __syncthreads();
+    if (!mbar_wait(&bar, 0)) {
+      if (threadIdx.x == 0) {
+        record_status(B.status, HGB_ERR_TIMEOUT);
+        mbar_wait(&bar, 0);  // the copy may still land: wait once more (bounded) before leaving
+      }
+      return;
+    }
+    const uint4 *src = reinterpret_cast<const uint4 *>(stage) + threadIdx.x * 4;
+    stg16(p.out + u * GB_UNIT + threadIdx.x * 16, gray_16(p, src[0], src[1], src[2], src[3]));
+    return;
+  }
+  // the pixels after the last whole unit (fewer than GB_UNIT)
+  for (int64_t i = B.nunits * GB_UNIT + threadIdx.x; i < B.npx; i += GB_T) {
+    const uint8_t *s = p.in + 4 * i;
+    const uint32_t rgba = (uint32_t)s[0] | ((uint32_t)s[1] << 8) | ((uint32_t)s[2] << 16) | ((uint32_t)s[3] << 24);
+    p.out[i] = (uint8_t)gray_px(p, rgba);
+  }
+}
+
 bool dense(const hgb_view &v) {
   const int64_t row = (int64_t)v.width * dtype_size(v.dtype);
   return v.pitch == row && (v.batch == 1 || v.batch_stride == row * v.height);
@@ -277,6 +336,20 @@ extern "C" int hgb_point_gray(const hgb_view *in, const hgb_view *out, int wr, i
   p.use_dp4a = wr < 256 && wg < 256 && wb < 256;
   p.wpack = (uint32_t)wr | ((uint32_t)wg << 8) | ((uint32_t)wb << 16);
   cudaStream_t st = (cudaStream_t)stream;
+  const int64_t npx = (int64_t)in->width * in->height * in->batch;
+  if (d && p.vec && npx >= (int64_t)GB_UNIT) {
+    // dense, 16-byte aligned: one bulk copy per CTA over the flat array
+    GrayBulkParams B;
+    B.p = p;
+    B.npx = npx;
+    B.nunits = npx / GB_UNIT;
+    B.status = device_status_word();
+    const int64_t g = B.nunits + (npx % GB_UNIT ? 1 : 0);
+    HGB_REQUIRE(g < (int64_t)0x7fffffff, "hgb_point_gray: image too large");
+    cudaEvent_t ev = before_launch(st);
+    gray_bulk_kernel<<<(unsigned)g, GB_T, 0, st>>>(B);
+    return after_launch("gray_bulk_kernel", st, ev);
+  }
   // one resident wave: every CTA owns one contiguous range
   static int per_sm = 0;
   if (!per_sm && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gray_kernel, 256, 0) != cudaSuccess)

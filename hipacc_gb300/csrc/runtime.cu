@@ -252,6 +252,15 @@ int hgb_image_read(const hgb_image *img, void *host, void *stream) {
   return HGB_OK;
 }
 
+int hgb_image_read_async(const hgb_image *img, void *host, void *stream) {
+  HGB_REQUIRE(img && host, "hgb_image_read_async: null argument");
+  const hgb_view &v = img->view;
+  const size_t row = (size_t)v.width * dtype_size(v.dtype);
+  HGB_CHECK_CUDA(cudaMemcpy2DAsync(host, row, v.data, v.pitch, row, v.height, cudaMemcpyDeviceToHost,
+                                   (cudaStream_t)stream));
+  return HGB_OK;
+}
+
 int hgb_image_copy(const hgb_image *src, hgb_image *dst, void *stream) {
   HGB_REQUIRE(src && dst, "hgb_image_copy: null argument");
   HGB_REQUIRE(src->view.width == dst->view.width && src->view.height == dst->view.height &&

@@ -213,10 +213,12 @@ __global__ void __launch_bounds__(SB_BX *SB_BY) sobel3_kernel(const __grid_const
 // Every warp runs its own two-stage pipeline (own shared-memory ring, own
 // mbarriers, no block-wide barrier): its lane 0 claims the next tile, issues
 // the load and the whole warp waits on that stage only.  CTA c owns tiles
-// c, c + G, c + 2G, ... (G CTAs, two per SM) and its 16 warps claim them from
+// c, c + G, c + 2G, ... (G CTAs, one per SM) and its 16 warps claim them from
 // a shared-memory counter, so SMs get equal shares and warps balance inside
 // the CTA.  Cells outside the image (TMA fills them with 0) are patched with
-// the boundary rule by the owning warp before use.
+// the boundary rule by the owning warp before use.  One CTA per SM (half the
+// SM's threads, 94 KB of shared memory) is as fast as two and leaves room for
+// an independent kernel of the same pipeline step to run alongside.
 //
 // Arithmetic is fp16x2 on exact integers: every intermediate (|gx|, |gy| <=
 // 1020, their sum <= 2040) is an integer below 2048 and therefore exact in
@@ -232,7 +234,7 @@ struct SobelTmaParams {
   unsigned int *ticket;
 };
 
-constexpr int T_TW = 128, T_TH = 16, T_WARPS = 16, T_NST = 2, T_CPS = 2;
+constexpr int T_TW = 128, T_TH = 16, T_WARPS = 16, T_NST = 2, T_CPS = 1;
 constexpr int T_SW = 160, T_SH = T_TH + 2, T_STAGE = T_SW * T_SH;
 constexpr int T_STAGE_PAD = (T_STAGE + 127) / 128 * 128;
 constexpr size_t T_SMEM = (size_t)T_WARPS * T_NST * T_STAGE_PAD + 128;  // + alignment slack
@@ -316,7 +318,8 @@ __device__ __forceinline__ void sobel_tile(const SobelParams &p, const uint8_t *
   }
 }
 
-__global__ void __launch_bounds__(T_WARPS * 32, T_CPS) sobel3_tma_kernel(const __grid_constant__ SobelTmaParams P) {
+// register budget of two CTAs per SM (64 per thread): the SM keeps room for a concurrent kernel
+__global__ void __launch_bounds__(T_WARPS * 32, 2) sobel3_tma_kernel(const __grid_constant__ SobelTmaParams P) {
   extern __shared__ __align__(128) uint8_t sobel_dsm[];
   __shared__ __align__(8) uint64_t bar[T_WARPS][T_NST];
   __shared__ int s_tile[T_WARPS][T_NST];

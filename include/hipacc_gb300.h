@@ -142,6 +142,11 @@ HGB_API int hgb_image_destroy(hgb_image *img);
 HGB_API int hgb_image_get_view(const hgb_image *img, hgb_view *out);
 HGB_API int hgb_image_write(hgb_image *img, const void *host, void *stream);
 HGB_API int hgb_image_read(const hgb_image *img, void *host, void *stream);
+/* hgb_image_read without the final stream synchronisation: the copy is
+ * queued on `stream` and `host` is valid once the stream reaches it (for
+ * pipelines that overlap one frame's read-back with the next frame's upload;
+ * no counterpart in the reference, whose hipaccReadMemory blocks). */
+HGB_API int hgb_image_read_async(const hgb_image *img, void *host, void *stream);
 HGB_API int hgb_image_copy(const hgb_image *src, hgb_image *dst, void *stream);
 HGB_API int hgb_image_copy_region(const hgb_image *src, const hgb_window *src_win, hgb_image *dst,
                           const hgb_window *dst_win, void *stream);

@@ -64,8 +64,10 @@ def test_sobel_repeated_calls_reset_ticket(gpu, oracle):
         assert s == int(oracle.sobel_mag(img, boundary=3).astype(np.uint64).sum())
 
 
-@pytest.mark.parametrize("hw", [(4096, 4096), (17, 33), (1, 5), (64, 1)])
+@pytest.mark.parametrize("hw", [(4096, 4096), (17, 33), (1, 5), (64, 1), (1000, 999), (5, 8192), (3, 1367)])
 def test_gray_bitexact(gpu, oracle, hw):
+    # dense images of at least one 4096-pixel unit take the bulk-copy pipeline
+    # (whole units + a ragged tail); smaller ones the vector kernel
     rng = np.random.default_rng(hw[0])
     rgba = rng.integers(0, 256, hw + (4,), dtype=np.uint8)
     t = torch.from_numpy(rgba).cuda()
