@@ -8,14 +8,15 @@
 // (dsl/kernel.hpp:121-161).  Integer arithmetic, so every order is exact.
 //
 // Fast path (the standard 3x3 Sobel masks, TMA-legal layout): sobel3_tma_kernel
-// below -- persistent CTAs, TMA double-buffered halo tiles, exact fp16x2
-// arithmetic.  Fallback for layouts TMA cannot address (unaligned base or
-// pitch): sobel3_kernel, which stages a 128 x 64 tile with 16-byte loads, walks
-// rows with a three-row register window and uses the separable form
-// gx = S(x+1) - S(x-1), S = top + 2 mid + bottom; gy = D(x-1) + 2 D(x) + D(x+1),
-// D = bottom - top.  Other masks: sobel_generic_kernel.  Every path reduces
-// sum and max with redux.sync across the warp, shared memory across the block
-// and a last-block combine of the per-block partials.
+// below -- one TMA-staged 128 x 128 tile per CTA, exact fp16x2 arithmetic, the
+// sum and max folded into workspace accumulators behind one ticket.  Fallback
+// for layouts TMA cannot address (unaligned base or pitch): sobel3_kernel,
+// which stages a 128 x 64 tile with 16-byte loads, walks rows with a three-row
+// register window and uses the separable form gx = S(x+1) - S(x-1),
+// S = top + 2 mid + bottom; gy = D(x-1) + 2 D(x) + D(x+1), D = bottom - top.
+// Other masks: sobel_generic_kernel.  The fallbacks reduce sum and max with
+// redux.sync across the warp, shared memory across the block and a last-block
+// combine of the per-block partials.
 #include <algorithm>
 
 #include "reduce_common.cuh"
@@ -208,17 +209,14 @@ __global__ void __launch_bounds__(SB_BX *SB_BY) sobel3_kernel(const __grid_const
 
 
 // ---------------------------------------------------------------------------
-// TMA path for the standard 3x3 masks.  Work unit: a 128 x 16 output tile,
-// staged as its 160 x 18 byte halo tile by one cp.async.bulk.tensor load.
-// Every warp runs its own two-stage pipeline (own shared-memory ring, own
-// mbarriers, no block-wide barrier): its lane 0 claims the next tile, issues
-// the load and the whole warp waits on that stage only.  CTA c owns tiles
-// c, c + G, c + 2G, ... (G CTAs, one per SM) and its 16 warps claim them from
-// a shared-memory counter, so SMs get equal shares and warps balance inside
-// the CTA.  Cells outside the image (TMA fills them with 0) are patched with
-// the boundary rule by the owning warp before use.  One CTA per SM (half the
-// SM's threads, 94 KB of shared memory) is as fast as two and leaves room for
-// an independent kernel of the same pipeline step to run alongside.
+// TMA path for the standard 3x3 masks.  One CTA per 128 x 128 output tile:
+// thread 0 loads the tile's 160 x 130 byte halo region with one
+// cp.async.bulk.tensor (completion on an mbarrier, bounded wait), and each of
+// the four warps runs 32 output rows of it, a lane owning four columns.  A CTA
+// holds 21 KB of shared memory and 128 threads, so an SM keeps up to ten tiles
+// in flight without a software pipeline, and independent kernels of the same
+// step can share the SMs.  Cells outside the image (TMA fills them with 0)
+// are patched with the boundary rule before use.
 //
 // Arithmetic is fp16x2 on exact integers: every intermediate (|gx|, |gy| <=
 // 1020, their sum <= 2040) is an integer below 2048 and therefore exact in
@@ -234,10 +232,9 @@ struct SobelTmaParams {
   unsigned int *ticket;
 };
 
-constexpr int T_TW = 128, T_TH = 16, T_WARPS = 16, T_NST = 2, T_CPS = 1;
+constexpr int T_TW = 128, T_R = 32, T_WARPS = 4, T_TH = T_R * T_WARPS;
 constexpr int T_SW = 160, T_SH = T_TH + 2, T_STAGE = T_SW * T_SH;
 constexpr int T_STAGE_PAD = (T_STAGE + 127) / 128 * 128;
-constexpr size_t T_SMEM = (size_t)T_WARPS * T_NST * T_STAGE_PAD + 128;  // + alignment slack
 
 __device__ __forceinline__ __half2 u2h(uint32_t u) {
   __half2 h;
@@ -318,123 +315,85 @@ __device__ __forceinline__ void sobel_tile(const SobelParams &p, const uint8_t *
   }
 }
 
-// register budget of two CTAs per SM (64 per thread): the SM keeps room for a concurrent kernel
-__global__ void __launch_bounds__(T_WARPS * 32, 2) sobel3_tma_kernel(const __grid_constant__ SobelTmaParams P) {
-  extern __shared__ __align__(128) uint8_t sobel_dsm[];
-  __shared__ __align__(8) uint64_t bar[T_WARPS][T_NST];
-  __shared__ int s_tile[T_WARPS][T_NST];
-  __shared__ int s_next;
+__global__ void __launch_bounds__(T_WARPS * 32) sobel3_tma_kernel(const __grid_constant__ SobelTmaParams P) {
+  __shared__ __align__(128) uint8_t tile[T_STAGE_PAD];
+  __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t s_sum[T_WARPS], s_max[T_WARPS];
   const SobelParams &p = P.p;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int G = gridDim.x, c = blockIdx.x;
-  const int n_c = c < P.ntiles ? (P.ntiles - c + G - 1) / G : 0;
-  if (threadIdx.x == 0) s_next = 0;
-  if (lane == 0) {
-    for (int s = 0; s < T_NST; ++s) mbar_init(&bar[warp][s], 1);
+  const int t = blockIdx.x;
+  const int tx_ = t % P.tiles_x, r_ = t / P.tiles_x;
+  const int i0 = tx_ * T_TW, j0 = (r_ % P.tiles_y) * T_TH, b = r_ / P.tiles_y;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
     mbar_fence_init();
+    mbar_expect_tx(&bar, T_STAGE);
+    tma_load_3d(tile, &P.map, i0 - 16, j0 - 1, b, &bar);
   }
   __syncthreads();
-  uint8_t *ring = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(sobel_dsm) + 127) & ~(uintptr_t)127) +
-                  warp * T_NST * T_STAGE_PAD;
-  auto coords = [&](int t, int &b, int &i0, int &j0) {
-    const int tx_ = t % P.tiles_x;
-    const int r = t / P.tiles_x;
-    j0 = (r % P.tiles_y) * T_TH;
-    b = r / P.tiles_y;
-    i0 = tx_ * T_TW;
-  };
-  // lane 0: claim the CTA's next tile and issue its load into stage st
-  auto claim_issue = [&](int st) {
-    int t = -1;
-    const int k = atomicAdd(&s_next, 1);
-    if (k < n_c) {
-      t = c + k * G;
-      int b, i0, j0;
-      coords(t, b, i0, j0);
-      fence_proxy_async_smem();
-      mbar_expect_tx(&bar[warp][st], T_STAGE);
-      tma_load_3d(ring + st * T_STAGE_PAD, &P.map, i0 - 16, j0 - 1, b, &bar[warp][st]);
+  if (!mbar_wait(&bar, 0)) {
+    if (threadIdx.x == 0) {
+      record_status(P.status, HGB_ERR_TIMEOUT);
+      mbar_wait(&bar, 0);  // the load may still land: wait once more (bounded) before leaving
     }
-    s_tile[warp][st] = t;
-  };
-  if (lane == 0)
-    for (int s = 0; s < T_NST; ++s) claim_issue(s);
-  __syncwarp();
+    // this CTA's partials are missing; the status word reports the launch as failed
+    if (p.sum_dev || p.max_dev)
+      if (threadIdx.x == 0) accumulate_and_publish(P.acc, P.acc + 1, P.ticket, 0, 0, p.sum_dev, p.max_dev);
+    return;
+  }
+  const int X0 = i0 - 16, Y0 = j0 - 1;
+  if (X0 + 15 < 0 || X0 + 145 > p.w || Y0 < 0 || Y0 + T_SH > p.h) {
+    // Patch the staged cells outside the image that the stencil reads
+    // (columns 15..144, all rows) with the boundary rule; TMA filled them
+    // with zeros.  Regions: left columns, right columns, top row, bottom rows.
+    const uint8_t *img = p.in + (int64_t)b * p.in_bstride;
+    constexpr int qa = 15, qb = 145, ncol = qb - qa;
+    const int nl = max(0, min(qb, -X0) - qa);
+    const int rs = max(qa, p.w - X0), nr = max(0, qb - rs);
+    const int ntop = max(0, -Y0);
+    const int bs = max(0, p.h - Y0), nb = max(0, T_SH - bs);
+    const int n1 = nl * T_SH, n2 = n1 + nr * T_SH, n3 = n2 + ntop * ncol, n4 = n3 + nb * ncol;
+    for (int cc = threadIdx.x; cc < n4; cc += T_WARPS * 32) {
+      int r, q;
+      if (cc < n1) {
+        r = cc / nl;
+        q = qa + (cc - r * nl);
+      } else if (cc < n2) {
+        const int d = cc - n1;
+        r = d / nr;
+        q = rs + (d - r * nr);
+      } else if (cc < n3) {
+        const int d = cc - n2;
+        r = d / ncol;
+        q = qa + (d - r * ncol);
+      } else {
+        const int d = cc - n3;
+        const int rr = d / ncol;
+        r = bs + rr;
+        q = qa + (d - rr * ncol);
+      }
+      tile[r * T_SW + q] = (uint8_t)sb_load_px(p, img, X0 + q, Y0 + r);
+    }
+    __syncthreads();
+  }
   uint32_t tsum = 0;
   __half2 tmax = __float2half2_rn(0.0f);
-  const int xs = 16 + 4 * lane;
-  for (int it = 0;; ++it) {
-    const int st = it % T_NST;
-    const int t = s_tile[warp][st];
-    if (t < 0) break;
-    const bool ok = mbar_wait(&bar[warp][st], (it / T_NST) & 1);
-    if (!__all_sync(0xffffffffu, ok)) {
-      if (lane == 0) {
-        record_status(P.status, HGB_ERR_TIMEOUT);
-        // the other stage may still have a load in flight: wait for it (bounded)
-        for (int j = 1; j < T_NST; ++j) {
-          const int s2 = (it + j) % T_NST;
-          if (s_tile[warp][s2] >= 0) mbar_wait(&bar[warp][s2], ((it + j) / T_NST) & 1);
-        }
-      }
-      break;
-    }
-    int b, i0, j0;
-    coords(t, b, i0, j0);
-    uint8_t *tile = ring + st * T_STAGE_PAD;
-    const int X0 = i0 - 16, Y0 = j0 - 1;
-    if (X0 + 15 < 0 || X0 + 145 > p.w || Y0 < 0 || Y0 + T_SH > p.h) {
-      // Patch the staged cells outside the image that the stencil reads
-      // (columns 15..144, all rows) with the boundary rule; TMA filled them
-      // with zeros.  Regions: left columns, right columns, top row, bottom rows.
-      const uint8_t *img = p.in + (int64_t)b * p.in_bstride;
-      constexpr int qa = 15, qb = 145, ncol = qb - qa;
-      const int nl = max(0, min(qb, -X0) - qa);
-      const int rs = max(qa, p.w - X0), nr = max(0, qb - rs);
-      const int ntop = max(0, -Y0);
-      const int bs = max(0, p.h - Y0), nb = max(0, T_SH - bs);
-      const int n1 = nl * T_SH, n2 = n1 + nr * T_SH, n3 = n2 + ntop * ncol, n4 = n3 + nb * ncol;
-      for (int cc = lane; cc < n4; cc += 32) {
-        int r, q;
-        if (cc < n1) {
-          r = cc / nl;
-          q = qa + (cc - r * nl);
-        } else if (cc < n2) {
-          const int d = cc - n1;
-          r = d / nr;
-          q = rs + (d - r * nr);
-        } else if (cc < n3) {
-          const int d = cc - n2;
-          r = d / ncol;
-          q = qa + (d - r * ncol);
-        } else {
-          const int d = cc - n3;
-          const int rr = d / ncol;
-          r = bs + rr;
-          q = qa + (d - rr * ncol);
-        }
-        tile[r * T_SW + q] = (uint8_t)sb_load_px(p, img, X0 + q, Y0 + r);
-      }
-      __syncwarp();
-    }
-    const int xo = i0 + 4 * lane;
-    uint8_t *out_row = p.out + (int64_t)b * p.out_bstride + (int64_t)j0 * p.out_pitch + xo;
-    if (p.vec_out && i0 + T_TW <= p.w && j0 + T_TH <= p.h)
-      sobel_tile<true, T_TH>(p, tile, out_row, xo, j0, xs, tsum, tmax);
+  const int xo = i0 + 4 * lane, jw = j0 + warp * T_R;
+  if (jw < p.h) {
+    uint8_t *out_row = p.out + (int64_t)b * p.out_bstride + (int64_t)jw * p.out_pitch + xo;
+    const uint8_t *wt = tile + warp * T_R * T_SW;
+    if (p.vec_out && i0 + T_TW <= p.w && jw + T_R <= p.h)
+      sobel_tile<true, T_R>(p, wt, out_row, xo, jw, 16 + 4 * lane, tsum, tmax);
     else
-      sobel_tile<false, T_TH>(p, tile, out_row, xo, j0, xs, tsum, tmax);
-    __syncwarp();  // the stage is read; refill it with this warp's next tile
-    if (lane == 0) claim_issue(st);
-    __syncwarp();
+      sobel_tile<false, T_R>(p, wt, out_row, xo, jw, 16 + 4 * lane, tsum, tmax);
   }
   if (p.sum_dev || p.max_dev) {
     const float2 mf = __half22float2(tmax);
-    const uint32_t bs = __reduce_add_sync(0xffffffffu, tsum);
-    const uint32_t bm = __reduce_max_sync(0xffffffffu, (uint32_t)fmaxf(mf.x, mf.y));
+    const uint32_t bsum = __reduce_add_sync(0xffffffffu, tsum);
+    const uint32_t bmax = __reduce_max_sync(0xffffffffu, (uint32_t)fmaxf(mf.x, mf.y));
     if (lane == 0) {
-      s_sum[warp] = bs;
-      s_max[warp] = bm;
+      s_sum[warp] = bsum;
+      s_max[warp] = bmax;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -549,17 +508,6 @@ extern "C" int hgb_sobel_mag(const hgb_view *in, const hgb_view *out, const int 
     rc = make_tensor_map_3d(&P.map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, in->data, p.w, p.h, in->batch, in->pitch,
                             in->batch_stride, T_SW, T_SH);
     if (rc == HGB_OK) {
-      // one resident wave: T_CPS CTAs per SM (fewer if the SM holds fewer)
-      static int per_sm = 0;
-      if (!per_sm) {
-        if (cudaFuncSetAttribute(sobel3_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T_SMEM) !=
-                cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sobel3_tma_kernel, T_WARPS * 32, T_SMEM) !=
-                cudaSuccess)
-          return set_error(HGB_ERR_CUDA, "hgb_sobel_mag: kernel attributes");
-        per_sm = std::max(1, std::min(per_sm, T_CPS));
-      }
-      const int g = std::max(1, std::min(P.ntiles, num_sms() * per_sm));
       if (sum_dev || max_dev) {
         Workspace ws;
         rc = workspace_get(0, &ws);
@@ -568,7 +516,7 @@ extern "C" int hgb_sobel_mag(const hgb_view *in, const hgb_view *out, const int 
         P.ticket = ws.tickets + 0;
       }
       cudaEvent_t ev = before_launch(st);
-      sobel3_tma_kernel<<<g, T_WARPS * 32, T_SMEM, st>>>(P);
+      sobel3_tma_kernel<<<P.ntiles, T_WARPS * 32, 0, st>>>(P);
       return after_launch("sobel3_tma_kernel", st, ev);
     }
   }
