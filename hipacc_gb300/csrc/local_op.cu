@@ -88,6 +88,9 @@ int fill_conv_params(const hgb_view &in, const hgb_window &acc, const hgb_view &
   p->is_h = is.height;
   p->bmode = boundary;
   p->cval = cval;
+  p->in_w = in.width;
+  p->in_h = in.height;
+  p->batch = in.batch;
   p->vec_in = ((uintptr_t)in.data % 16 == 0) && (in.pitch % 16 == 0) && (in.batch_stride % 16 == 0 || in.batch == 1) &&
               (acc.offset_x % vec_elems(in.dtype) == 0);
   p->vec_out = ((uintptr_t)out.data % 16 == 0) && (out.pitch % 16 == 0) &&
@@ -135,6 +138,11 @@ extern "C" int hgb_local_op(const hgb_view *in, const hgb_window *accw, const hg
         const float m = mask ? mask[y * mask_w + x] : 1.0f;
         p.mask[(y + dy) * kw + (x + dx)] = on ? m : 0.0f;
       }
+    for (int i = 0; i < kw * kh; ++i) {
+      uint32_t bits;
+      memcpy(&bits, &p.mask[i], 4);
+      p.mask2[i] = ((f2)bits << 32) | bits;
+    }
     return run_conv(in->dtype, out->dtype, p, kw, kh, in->batch, st);
   }
   GenParams g;

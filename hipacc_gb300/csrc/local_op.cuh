@@ -7,21 +7,30 @@
 // boundary remap (lib/AST/BorderHandling.cpp:124-407).
 //
 // GB300 design: a CTA computes a TW x TH output tile.  Its input tile plus
-// halo is staged once in shared memory as FP32 with 16-byte global loads; only
-// the chunks that leave the accessor window are remapped element by element.
-// Each thread keeps a PX x PY block of outputs in registers and streams the
-// input rows of its column window through registers, so every staged value
-// feeds up to PX*MW*... FMAs.  SUM uses fused multiply-add in the row-major
-// tap order, which is the contracted form of the reference's `_tmp += m*x`.
+// halo is staged once in shared memory as FP32: for FP32 images read through
+// the whole-image accessor by one cp.async.bulk.tensor load (cells outside the
+// image, which TMA fills with zeros, are then patched with the boundary rule),
+// otherwise with 16-byte global loads, remapping element by element only the
+// chunks that leave the accessor window.  Each thread keeps a PX x PY block of
+// outputs in registers as horizontal pairs and streams the input rows of its
+// column window through registers; every tap is one packed f32x2 fused
+// multiply-add for two outputs.  SUM keeps the row-major tap order per output,
+// the contracted form of the reference's `_tmp += m*x`, bit for bit.
 #pragma once
 
-#include "hgb_internal.cuh"
+#include <type_traits>
+
+#include "tma.cuh"
 
 namespace hgb {
 
 constexpr int kMaxMask = 15;
 
 struct ConvParams {
+  CUtensorMap map;                   // FP32 input, whole image: TMA staging when use_tma
+  int use_tma;
+  int *status;
+  int in_w, in_h, batch;             // input image size (tensor-map extent)
   const char *in;
   int64_t in_pitch, in_bstride;
   char *out;
@@ -32,6 +41,7 @@ struct ConvParams {
   float cval;
   int vec_in, vec_out;               // 16-byte vector access legal
   float mask[kMaxMask * kMaxMask];   // row-major, padded shape
+  f2 mask2[kMaxMask * kMaxMask];     // the same coefficients as (m, m) pairs for f32x2 FMAs
 };
 
 struct TileCfg {
@@ -53,7 +63,8 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
   constexpr int SH = TH + MH - 1;
   constexpr int CPR = SW / VI;
   static_assert(TW % VI == 0 && SW % 4 == 0 && PX % 4 == 0, "tile shape");
-  __shared__ __align__(16) float tile[SH * SW];
+  __shared__ __align__(128) float tile[SH * SW];
+  __shared__ __align__(8) uint64_t bar;
 
   const int b = blockIdx.z;
   const int i0 = blockIdx.x * TW, j0 = blockIdx.y * TH;
@@ -65,7 +76,53 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
 
   // ---- stage input tile + halo as FP32
   const bool interior = X0 >= ax_lo && X0 + SW <= ax_hi && Y0 >= ay_lo && Y0 + SH <= ay_hi;
-  if (interior && p.vec_in) {
+  if (std::is_same<TI, float>::value && p.use_tma) {
+    // the accessor window is the whole image: one TMA load of the box
+    if (threadIdx.x == 0) {
+      mbar_init(&bar, 1);
+      mbar_fence_init();
+      mbar_expect_tx(&bar, SH * SW * 4);
+      tma_load_3d(tile, &p.map, X0, Y0, b, &bar);
+    }
+    __syncthreads();
+    if (!mbar_wait(&bar, 0)) {
+      if (threadIdx.x == 0) {
+        record_status(p.status, HGB_ERR_TIMEOUT);
+        mbar_wait(&bar, 0);  // the load may still land: wait once more (bounded) before leaving
+      }
+      return;
+    }
+    if (!interior) {
+      // cells outside the image (zero-filled by TMA): left / right columns, top / bottom rows
+      const int nl = max(0, min(SW, ax_lo - X0)), rs = max(0, min(SW, ax_hi - X0));
+      const int nt = max(0, min(SH, ay_lo - Y0)), bs = max(0, min(SH, ay_hi - Y0));
+      const int ncl = nl * SH, ncr = (SW - rs) * SH, nrt = nt * SW, nrb = (SH - bs) * SW;
+      for (int c = threadIdx.x; c < ncl + ncr + nrt + nrb; c += NT) {
+        int r, q;
+        if (c < ncl) {
+          r = c / nl;
+          q = c - r * nl;
+        } else if (c < ncl + ncr) {
+          const int d = c - ncl, n = SW - rs;
+          r = d / n;
+          q = rs + (d - r * n);
+        } else if (c < ncl + ncr + nrt) {
+          const int d = c - ncl - ncr;
+          r = d / SW;
+          q = d - r * SW;
+        } else {
+          const int d = c - ncl - ncr - nrt;
+          const int rr = d / SW;
+          r = bs + rr;
+          q = d - rr * SW;
+        }
+        const int ry = remap(p.bmode, Y0 + r, ay_lo, ay_hi), rx = remap(p.bmode, X0 + q, ax_lo, ax_hi);
+        tile[r * SW + q] = (ry == (int)0x80000000 || rx == (int)0x80000000)
+                               ? p.cval
+                               : Storage<TI>::load(reinterpret_cast<const TI *>(in + (int64_t)ry * p.in_pitch) + rx);
+      }
+    }
+  } else if (interior && p.vec_in) {
 #pragma unroll 4
     for (int c = threadIdx.x; c < SH * CPR; c += NT) {
       const int r = c / CPR, k = c - r * CPR;
@@ -105,11 +162,12 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
   constexpr int OFF = (HL - RX) % 4;
   constexpr int NV = cdiv(OFF + PX + MW - 1, 4);
   const int cbase = HL - RX - OFF + tx * PX;
-  float acc[PY][PX];
+  constexpr int NP = PX / 2;
+  f2 acc2[PY][NP];
 #pragma unroll
   for (int oy = 0; oy < PY; ++oy)
 #pragma unroll
-    for (int px = 0; px < PX; ++px) acc[oy][px] = 0.0f;
+    for (int pp = 0; pp < NP; ++pp) acc2[oy][pp] = 0ull;
 
 #pragma unroll
   for (int r = 0; r < PY + MH - 1; ++r) {
@@ -123,16 +181,36 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
       win[4 * v + 2] = t.z;
       win[4 * v + 3] = t.w;
     }
+    // window pairs starting at even (E) and odd (O) positions
+    f2 E[NV * 2], O[NV * 2];
+#pragma unroll
+    for (int j = 0; j < NV * 2; ++j) {
+      E[j] = f2_pack(win[2 * j], win[2 * j + 1]);
+      O[j] = f2_pack(win[2 * j + 1], 2 * j + 2 < NV * 4 ? win[2 * j + 2] : 0.0f);
+    }
 #pragma unroll
     for (int oy = 0; oy < PY; ++oy) {
       const int my = r - oy;
       if (my < 0 || my >= MH) continue;
 #pragma unroll
-      for (int px = 0; px < PX; ++px)
+      for (int mx = 0; mx < MW; ++mx) {
+        const f2 m2 = p.mask2[my * MW + mx];
 #pragma unroll
-        for (int mx = 0; mx < MW; ++mx) acc[oy][px] = __fmaf_rn(p.mask[my * MW + mx], win[OFF + px + mx], acc[oy][px]);
+        for (int pp = 0; pp < NP; ++pp) {
+          const int st = OFF + 2 * pp + mx;  // window position of the pair's first output
+          acc2[oy][pp] = f2_fma(m2, (st & 1) ? O[st >> 1] : E[st >> 1], acc2[oy][pp]);
+        }
+      }
     }
   }
+  float acc[PY][PX];
+#pragma unroll
+  for (int oy = 0; oy < PY; ++oy)
+#pragma unroll
+    for (int pp = 0; pp < NP; ++pp) {
+      acc[oy][2 * pp] = f2_lo(acc2[oy][pp]);
+      acc[oy][2 * pp + 1] = f2_hi(acc2[oy][pp]);
+    }
 
   // ---- store
   char *out = p.out + (int64_t)b * p.out_bstride;
@@ -173,8 +251,22 @@ struct GenParams {
   uint8_t domain[kMaxMask * kMaxMask];
 };
 
+// square K x K kernels, instantiated per (storage type, K) in the lop_sq_* translation units
+template <typename TI, typename TO, int K>
+int launch_conv_sq(const ConvParams &p, int batch, cudaStream_t st, int cfg_index);
 template <typename TI, typename TO>
-int launch_conv_square(const ConvParams &p, int mw, int mh, int batch, cudaStream_t st, int cfg_index);
+int launch_conv_square(const ConvParams &p, int mw, int mh, int batch, cudaStream_t st, int cfg_index) {
+  (void)mh;
+  switch (mw) {
+    case 3: return launch_conv_sq<TI, TO, 3>(p, batch, st, cfg_index);
+    case 5: return launch_conv_sq<TI, TO, 5>(p, batch, st, cfg_index);
+    case 7: return launch_conv_sq<TI, TO, 7>(p, batch, st, cfg_index);
+    case 9: return launch_conv_sq<TI, TO, 9>(p, batch, st, cfg_index);
+    case 11: return launch_conv_sq<TI, TO, 11>(p, batch, st, cfg_index);
+    case 13: return launch_conv_sq<TI, TO, 13>(p, batch, st, cfg_index);
+  }
+  return set_error(HGB_ERR_UNSUPPORTED, "conv: no fast kernel for this mask shape");
+}
 template <typename TI, typename TO>
 int launch_conv_line(const ConvParams &p, int mw, int mh, int batch, cudaStream_t st, int cfg_index);
 template <typename TI, typename TO>

@@ -13,8 +13,20 @@ namespace hgb {
   X(2, 32, 4, 4, 8)
 
 template <typename TI, typename TO, int MW, int MH, int BX, int BY, int PX, int PY>
-int launch_cfg(const ConvParams &p, int batch, cudaStream_t st) {
+int launch_cfg(const ConvParams &p0, int batch, cudaStream_t st) {
   constexpr int TW = BX * PX, TH = BY * PY;
+  constexpr int RX = MW / 2, VI = Vec16<TI>::N;
+  constexpr int SW = round_up(RX, VI) + TW + round_up(MW - 1 - RX, VI), SH = TH + MH - 1;
+  ConvParams p = p0;
+  // FP32 images read through the whole-image accessor stage their tiles with TMA
+  p.use_tma = 0;
+  if (std::is_same<TI, float>::value && p.acc_ox == 0 && p.acc_oy == 0 && p.acc_w == p.in_w && p.acc_h == p.in_h &&
+      tma_legal(p.in, p.in_pitch, p.in_bstride, batch) &&
+      make_tensor_map_3d(&p.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p.in, p.in_w, p.in_h, batch, p.in_pitch,
+                         p.in_bstride, SW, SH) == HGB_OK) {
+    p.use_tma = 1;
+    p.status = device_status_word();
+  }
   dim3 grid(cdiv(p.is_w, TW), cdiv(p.is_h, TH), batch);
   cudaEvent_t ev = before_launch(st);
   conv_kernel<TI, TO, MW, MH, BX, BY, PX, PY><<<grid, BX * BY, 0, st>>>(p);
@@ -23,23 +35,25 @@ int launch_cfg(const ConvParams &p, int batch, cudaStream_t st) {
 
 template <typename TI, typename TO, int MW, int MH>
 int launch_shape(const ConvParams &p, int batch, cudaStream_t st, int cfg) {
-  switch (cfg) {
+  // masks of 9 x 9 and larger are FMA-bound in every tile shape: one configuration
+  if constexpr (MW * MH >= 81) {
+    (void)cfg;
+    return launch_cfg<TI, TO, MW, MH, 16, 8, 4, 8>(p, batch, st);
+  } else {
+    switch (cfg) {
 #define HGB_CFG_CASE(I, BX, BY, PX, PY) \
   case I: return launch_cfg<TI, TO, MW, MH, BX, BY, PX, PY>(p, batch, st);
-    HGB_TILE_CFGS(HGB_CFG_CASE)
+      HGB_TILE_CFGS(HGB_CFG_CASE)
 #undef HGB_CFG_CASE
+    }
+    return set_error(HGB_ERR_INVALID, "conv: bad tile configuration");
   }
-  return set_error(HGB_ERR_INVALID, "conv: bad tile configuration");
 }
 
-// square masks (one translation unit per storage type) ...
-template <typename TI, typename TO>
-int launch_conv_square(const ConvParams &p, int mw, int mh, int batch, cudaStream_t st, int cfg) {
-#define HGB_SQ(K) \
-  if (mw == K && mh == K) return launch_shape<TI, TO, K, K>(p, batch, st, cfg);
-  HGB_SQ(3) HGB_SQ(5) HGB_SQ(7) HGB_SQ(9) HGB_SQ(11) HGB_SQ(13)
-#undef HGB_SQ
-  return set_error(HGB_ERR_UNSUPPORTED, "conv: no fast kernel for this mask shape");
+// square masks (translation units per storage type and group of sizes) ...
+template <typename TI, typename TO, int K>
+int launch_conv_sq(const ConvParams &p, int batch, cudaStream_t st, int cfg) {
+  return launch_shape<TI, TO, K, K>(p, batch, st, cfg);
 }
 
 // ... and 1xK / Kx1 masks (another one), so that they compile in parallel
@@ -127,9 +141,7 @@ int launch_generic(const GenParams &g, int batch, cudaStream_t st) {
   return after_launch("generic_kernel", st, ev);
 }
 
-#define HGB_INSTANTIATE_SQUARE(TI, TO)                                                              \
-  template int launch_conv_square<TI, TO>(const ConvParams &, int, int, int, cudaStream_t, int);    \
-  template int launch_generic<TI, TO>(const GenParams &, int, cudaStream_t);
+#define HGB_INSTANTIATE_SQ(TI, TO, K) template int launch_conv_sq<TI, TO, K>(const ConvParams &, int, cudaStream_t, int);
 #define HGB_INSTANTIATE_LINE(TI, TO) \
   template int launch_conv_line<TI, TO>(const ConvParams &, int, int, int, cudaStream_t, int);
 #define HGB_INSTANTIATE_GENERIC(TI, TO) template int launch_generic<TI, TO>(const GenParams &, int, cudaStream_t);
