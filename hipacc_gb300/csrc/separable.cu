@@ -15,7 +15,18 @@
 //     remapped input row (which is what the staged halo rows hold), and for
 //     CONSTANT the constant itself.
 // Storage f32 / bf16 / f16 in and out (same type), FP32 arithmetic.
+//
+// GB300 form: a TMA-legal image (16-byte aligned base, pitch and batch
+// stride) is staged by one cp.async.bulk.tensor load per CTA in its storage
+// type (bf16 / f16 tiles are then widened to FP32 in shared memory); cells
+// outside the image, which TMA fills with zeros, are patched with the boundary
+// rule.  Other layouts stage with 16-byte global loads.  Both passes run
+// packed f32x2 fused multiply-adds on pairs of adjacent outputs, keeping each
+// output's tap order.
+#include <type_traits>
+
 #include "stage.cuh"
+#include "tma.cuh"
 
 namespace hgb {
 namespace {
@@ -23,6 +34,9 @@ namespace {
 constexpr int kSepMaxK = 15;
 
 struct SepParams {
+  CUtensorMap map;  // storage-type tensor map of the input when use_tma
+  int use_tma;
+  int *status;
   const char *in;
   int64_t in_pitch, in_bstride;
   char *out;
@@ -32,6 +46,7 @@ struct SepParams {
   float cval;
   int vec_in, vec_out;
   float row[kSepMaxK], col[kSepMaxK];
+  f2 row2[kSepMaxK], col2[kSepMaxK];  // the same taps as (t, t) pairs
 };
 
 constexpr int SP_BX = 32, SP_BY = 8, SP_PX = 4, SP_PY = 4;
@@ -44,20 +59,85 @@ struct SepShape {
   static constexpr int HL = round_up(R, VI);
   static constexpr int SW = HL + SP_TW + round_up(R, VI);
   static constexpr int SH = SP_TH + K - 1;
-  static constexpr size_t smem = sizeof(float) * ((size_t)SH * SW + (size_t)SH * SP_TW);
+  // raw storage-type tile (TMA destination; bf16 / f16 only), FP32 tile, row-pass buffer
+  static constexpr size_t raw = std::is_same<T, float>::value ? 0 : (((size_t)SH * SW * sizeof(T) + 127) / 128 * 128);
+  static constexpr size_t smem = raw + sizeof(float) * ((size_t)SH * SW + (size_t)SH * SP_TW) + 128;
 };
 
 template <typename T, int K>
 __global__ void __launch_bounds__(SP_BX *SP_BY) separable_kernel(const __grid_constant__ SepParams p) {
   using S = SepShape<T, K>;
   constexpr int R = S::R, HL = S::HL, SW = S::SW, SH = S::SH;
-  extern __shared__ __align__(16) float smem[];
-  float *tile = smem;
-  float *rowb = smem + SH * SW;
+  constexpr int NT = SP_BX * SP_BY;
+  extern __shared__ __align__(128) uint8_t sep_dsm[];
+  __shared__ __align__(8) uint64_t bar;
+  uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(sep_dsm) + 127) & ~(uintptr_t)127);
+  T *raw = reinterpret_cast<T *>(base);
+  float *tile = reinterpret_cast<float *>(base + S::raw);
+  float *rowb = tile + SH * SW;
   const int b = blockIdx.z;
   const int i0 = blockIdx.x * SP_TW, j0 = blockIdx.y * SP_TH;
-  stage_tile<T, SW, SH, SP_BX * SP_BY>(tile, p.in + (int64_t)b * p.in_bstride, p.in_pitch, i0 - HL, j0 - R, 0, p.w,
-                                        0, p.h, p.bmode, p.cval, p.vec_in);
+  const int X0 = i0 - HL, Y0 = j0 - R;
+  const char *img = p.in + (int64_t)b * p.in_bstride;
+  if (p.use_tma) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bar, 1);
+      mbar_fence_init();
+      mbar_expect_tx(&bar, SH * SW * (int)sizeof(T));
+      tma_load_3d(std::is_same<T, float>::value ? (void *)tile : (void *)raw, &p.map, X0, Y0, b, &bar);
+    }
+    __syncthreads();
+    if (!mbar_wait(&bar, 0)) {
+      if (threadIdx.x == 0) {
+        record_status(p.status, HGB_ERR_TIMEOUT);
+        mbar_wait(&bar, 0);  // the load may still land: wait once more (bounded) before leaving
+      }
+      return;
+    }
+    if constexpr (!std::is_same<T, float>::value) {
+      // widen the staged tile to FP32, 8 elements per 16-byte chunk
+      constexpr int NCH = SH * SW / 8;
+      for (int c = threadIdx.x; c < NCH; c += NT) {
+        float f[8];
+        Vec16<T>::unpack(reinterpret_cast<const uint4 *>(raw)[c], f);
+        *reinterpret_cast<float4 *>(&tile[8 * c]) = make_float4(f[0], f[1], f[2], f[3]);
+        *reinterpret_cast<float4 *>(&tile[8 * c + 4]) = make_float4(f[4], f[5], f[6], f[7]);
+      }
+    }
+    if (X0 < 0 || X0 + SW > p.w || Y0 < 0 || Y0 + SH > p.h) {
+      if constexpr (!std::is_same<T, float>::value) __syncthreads();
+      // cells outside the image (zero-filled by TMA): left / right columns, top / bottom rows
+      const int nl = max(0, min(SW, -X0)), rs = max(0, min(SW, p.w - X0));
+      const int nt = max(0, min(SH, -Y0)), bs = max(0, min(SH, p.h - Y0));
+      const int ncl = nl * SH, ncr = (SW - rs) * SH, nrt = nt * SW, nrb = (SH - bs) * SW;
+      for (int c = threadIdx.x; c < ncl + ncr + nrt + nrb; c += NT) {
+        int r, q;
+        if (c < ncl) {
+          r = c / nl;
+          q = c - r * nl;
+        } else if (c < ncl + ncr) {
+          const int d = c - ncl, n = SW - rs;
+          r = d / n;
+          q = rs + (d - r * n);
+        } else if (c < ncl + ncr + nrt) {
+          const int d = c - ncl - ncr;
+          r = d / SW;
+          q = d - r * SW;
+        } else {
+          const int d = c - ncl - ncr - nrt;
+          const int rr = d / SW;
+          r = bs + rr;
+          q = d - rr * SW;
+        }
+        const int ry = remap(p.bmode, Y0 + r, 0, p.h), rx = remap(p.bmode, X0 + q, 0, p.w);
+        tile[r * SW + q] = (ry == (int)0x80000000 || rx == (int)0x80000000)
+                               ? p.cval
+                               : Storage<T>::load(reinterpret_cast<const T *>(img + (int64_t)ry * p.in_pitch) + rx);
+      }
+    }
+  } else {
+    stage_tile<T, SW, SH, NT>(tile, img, p.in_pitch, X0, Y0, 0, p.w, 0, p.h, p.bmode, p.cval, p.vec_in);
+  }
   __syncthreads();
   const int tx = threadIdx.x % SP_BX, ty = threadIdx.x / SP_BX;
   // ---- row pass: 4 outputs per thread per staged row
@@ -75,12 +155,27 @@ __global__ void __launch_bounds__(SP_BX *SP_BY) separable_kernel(const __grid_co
         win[4 * v + 2] = t.z;
         win[4 * v + 3] = t.w;
       }
+      f2 E[NV * 2], O[NV * 2];
+#pragma unroll
+      for (int j = 0; j < NV * 2; ++j) {
+        E[j] = f2_pack(win[2 * j], win[2 * j + 1]);
+        O[j] = f2_pack(win[2 * j + 1], 2 * j + 2 < NV * 4 ? win[2 * j + 2] : 0.0f);
+      }
+      f2 a2[SP_PX / 2];
+#pragma unroll
+      for (int pp = 0; pp < SP_PX / 2; ++pp) {
+        a2[pp] = 0ull;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const int st = OFF + 2 * pp + k;
+          a2[pp] = f2_fma(p.row2[k], (st & 1) ? O[st >> 1] : E[st >> 1], a2[pp]);
+        }
+      }
       float acc[SP_PX];
 #pragma unroll
-      for (int px = 0; px < SP_PX; ++px) {
-        acc[px] = 0.0f;
-#pragma unroll
-        for (int k = 0; k < K; ++k) acc[px] = __fmaf_rn(p.row[k], win[OFF + px + k], acc[px]);
+      for (int pp = 0; pp < SP_PX / 2; ++pp) {
+        acc[2 * pp] = f2_lo(a2[pp]);
+        acc[2 * pp + 1] = f2_hi(a2[pp]);
       }
       const int ay = j0 - R + r;
       if (p.bmode == HGB_BOUNDARY_CONSTANT && (ay < 0 || ay >= p.h))
@@ -91,23 +186,31 @@ __global__ void __launch_bounds__(SP_BX *SP_BY) separable_kernel(const __grid_co
   }
   __syncthreads();
   // ---- column pass: 4 x 4 outputs per thread
-  float acc[SP_PY][SP_PX];
+  f2 c2[SP_PY][SP_PX / 2];
 #pragma unroll
   for (int oy = 0; oy < SP_PY; ++oy)
 #pragma unroll
-    for (int px = 0; px < SP_PX; ++px) acc[oy][px] = 0.0f;
+    for (int pp = 0; pp < SP_PX / 2; ++pp) c2[oy][pp] = 0ull;
 #pragma unroll
   for (int r = 0; r < SP_PY + K - 1; ++r) {
     const float4 t = *reinterpret_cast<const float4 *>(&rowb[(ty * SP_PY + r) * SP_TW + tx * SP_PX]);
-    const float v[4] = {t.x, t.y, t.z, t.w};
+    const f2 v01 = f2_pack(t.x, t.y), v23 = f2_pack(t.z, t.w);
 #pragma unroll
     for (int oy = 0; oy < SP_PY; ++oy) {
       const int k = r - oy;
       if (k < 0 || k >= K) continue;
-#pragma unroll
-      for (int px = 0; px < SP_PX; ++px) acc[oy][px] = __fmaf_rn(p.col[k], v[px], acc[oy][px]);
+      c2[oy][0] = f2_fma(p.col2[k], v01, c2[oy][0]);
+      c2[oy][1] = f2_fma(p.col2[k], v23, c2[oy][1]);
     }
   }
+  float acc[SP_PY][SP_PX];
+#pragma unroll
+  for (int oy = 0; oy < SP_PY; ++oy)
+#pragma unroll
+    for (int pp = 0; pp < SP_PX / 2; ++pp) {
+      acc[oy][2 * pp] = f2_lo(c2[oy][pp]);
+      acc[oy][2 * pp + 1] = f2_hi(c2[oy][pp]);
+    }
   char *out = p.out + (int64_t)b * p.out_bstride;
   const int i = i0 + tx * SP_PX;
 #pragma unroll
@@ -118,9 +221,25 @@ __global__ void __launch_bounds__(SP_BX *SP_BY) separable_kernel(const __grid_co
   }
 }
 
+template <typename T>
+constexpr CUtensorMapDataType tma_dtype() {
+  return std::is_same<T, float>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+         : std::is_same<T, __half>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                          : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+}
+
 template <typename T, int K>
-int launch_sep_k(const SepParams &p, int batch, cudaStream_t st) {
-  constexpr size_t smem = SepShape<T, K>::smem;
+int launch_sep_k(const SepParams &p0, int batch, cudaStream_t st) {
+  using S = SepShape<T, K>;
+  constexpr size_t smem = S::smem;
+  SepParams p = p0;
+  p.use_tma = 0;
+  if (tma_legal(p.in, p.in_pitch, p.in_bstride, batch) &&
+      make_tensor_map_3d(&p.map, tma_dtype<T>(), (int)sizeof(T), p.in, p.w, p.h, batch, p.in_pitch, p.in_bstride,
+                         S::SW, S::SH) == HGB_OK) {
+    p.use_tma = 1;
+    p.status = device_status_word();
+  }
   static bool attr = false;
   if (!attr) {
     HGB_CHECK_CUDA(cudaFuncSetAttribute(separable_kernel<T, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -180,6 +299,11 @@ extern "C" int hgb_separable(const hgb_view *in, const hgb_view *out, const floa
   for (int i = 0; i < k; ++i) {
     p.row[i] = row_taps[i];
     p.col[i] = col_taps[i];
+    uint32_t rb, cb;
+    memcpy(&rb, &p.row[i], 4);
+    memcpy(&cb, &p.col[i], 4);
+    p.row2[i] = ((f2)rb << 32) | rb;
+    p.col2[i] = ((f2)cb << 32) | cb;
   }
   cudaStream_t st = (cudaStream_t)stream;
   switch (in->dtype) {
