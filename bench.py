@@ -408,7 +408,7 @@ def gauss_taps(k, sigma):
     return (g / g.sum()).astype(np.float32)
 
 
-OTHER_SECTIONS = ("gaussian", "precision", "pyramid", "diff")
+OTHER_SECTIONS = ("gaussian", "precision", "pyramid", "diff", "histogram")
 
 
 def measure_other_configs(dev, peak_gbs, only=None):
@@ -433,7 +433,30 @@ def measure_other_configs(dev, peak_gbs, only=None):
         _pyramid(dev, peak_gbs, s, res, q)
     if want("diff"):
         _diff(dev, s, res, q)
+    if want("histogram"):
+        _histogram(dev, peak_gbs, s, res, q)
     return res
+
+
+def _histogram(dev, peak_gbs, s, res, q):
+    import torch
+
+    from hipacc_gb300 import api
+
+    # binned data of the histogram binning function, 256 bins, 4096x4096 u8 and f32
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    px = 4096 * 4096
+    for name, make, es in (("u8", lambda: torch.randint(0, 256, (4096, 4096), dtype=torch.uint8, device=dev,
+                                                        generator=g), 1),
+                           ("f32", lambda: torch.rand((4096, 4096), device=dev, generator=g) * 255.0, 4)):
+        ins = [make() for _ in range(8)]
+        bins = [torch.empty(256, dtype=torch.int32, device=dev) for _ in range(8)]
+        us = graph_time_us(lambda i: api.histogram(ins[i], 256, bins=bins[i], stream=s), 8, s, 2 if q else 20)
+        res[f"histogram256_{name}_4096"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                            "achieved_gbs": es * px / us / 1e3,
+                                            "frac_hbm": es * px / us / 1e3 / peak_gbs}
+        del ins
 
 
 def _gaussian(dev, peak_gbs, s, res, q):

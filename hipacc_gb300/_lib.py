@@ -62,6 +62,7 @@ SIGNATURES = {
     "hgb_image_write": (i32, [vp, vp, vp]),
     "hgb_image_read": (i32, [vp, vp, vp]),
     "hgb_image_read_async": (i32, [vp, vp, vp]),
+    "hgb_histogram": (i32, [vp, vp, C.c_uint, vp, vp, vp]),
     "hgb_image_copy": (i32, [vp, vp, vp]),
     "hgb_image_copy_region": (i32, [vp, WP, vp, WP, vp]),
     "hgb_local_op": (i32, [VP, WP, VP, WP, vp, vp, vp, i32, i32, i32, i32, f32, vp]),

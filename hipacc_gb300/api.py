@@ -158,6 +158,16 @@ def reduce(inp, op=SUM, win=None, result_dev=None, stream=None):
     return struct.unpack("<Q", raw)[0]
 
 
+def histogram(inp, num_bins, win=None, bins=None, stream=None):
+    """Binned data of the histogram binning function (uint32 bins on the device)."""
+    if bins is None:
+        bins = torch.empty(num_bins, dtype=torch.int32, device=inp.device)
+    vi = view(inp)
+    L.call("hgb_histogram", C.byref(vi), window(win), int(num_bins), C.c_void_p(bins.data_ptr()), None,
+           _stream(stream))
+    return bins
+
+
 def separable(inp, out=None, row_taps=None, col_taps=None, boundary=CLAMP, const=0.0, stream=None):
     if out is None:
         out = torch.empty_like(inp)

@@ -1,0 +1,170 @@
+// binning.cu -- hgb_histogram: binned data of the histogram binning kernel.
+//
+// Reference: Kernel::binned_data (dsl/kernel.hpp:163-200) with the binning
+// function of samples-public/2_Global_Operators/Histogram/src/main.cpp:41-47,
+//   bin((unsigned)(pixel / 255.0f * num_bins)) = 1,  reduce = left + right,
+// run on the GPU by hipaccApplyBinningSegmented (runtime/hipacc_cu.tpp:410-464,
+// device code runtime/hipacc_cu_red.hpp:527-641) and on the CPU by
+// BINNING_CPU_2D (runtime/hipacc_cpu_red.hpp:70-126), whose Put drops bin
+// indices past the last bin.  The float-to-unsigned conversion here saturates
+// (negative and NaN products land in bin 0), where C leaves it undefined.
+//
+// GB300 form: one resident wave of CTAs, each with a private histogram in
+// shared memory (shared-memory atomics), the image read as 16-pixel chunks
+// with 16-byte loads where the layout allows, and one global atomic add per
+// non-empty private bin at the end.  Integer sums, so the result does not
+// depend on the order.  u8 pixels map through a 256-entry table computed
+// with the same float arithmetic.
+#include <algorithm>
+
+#include "hgb_internal.cuh"
+
+namespace hgb {
+namespace {
+
+constexpr int HB_T = 256;
+constexpr unsigned kMaxBins = 16384;
+
+struct HistParams {
+  const char *in;
+  int64_t pitch, bstride;
+  int ox, oy, w, h, batch;
+  int es;      // element size (1: u8, 4: f32)
+  int dense;   // window rows back to back over the batch: one flat run
+  int vec;     // 16-byte loads legal for every chunk
+  unsigned nb;
+  uint32_t *bins;
+};
+
+__device__ __forceinline__ uint32_t bin_of(float px, unsigned nb) {
+  // pixel / 255 * num_bins with the sample's two roundings, truncated
+  return __float2uint_rz(__fmul_rn(__fdiv_rn(px, 255.0f), (float)nb));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(HB_T) hist_kernel(const __grid_constant__ HistParams p) {
+  extern __shared__ uint32_t hist_smem[];
+  uint32_t *sb = hist_smem;
+  uint32_t *lut = hist_smem + p.nb;  // u8 only
+  for (unsigned i = threadIdx.x; i < p.nb; i += HB_T) sb[i] = 0u;
+  if constexpr (sizeof(T) == 1)
+    for (int v = threadIdx.x; v < 256; v += HB_T) lut[v] = bin_of((float)v, p.nb);
+  __syncthreads();
+  auto put = [&](T px) {
+    uint32_t idx;
+    if constexpr (sizeof(T) == 1)
+      idx = lut[(uint32_t)px];
+    else
+      idx = bin_of((float)px, p.nb);
+    if (idx < p.nb) atomicAdd(&sb[idx], 1u);
+  };
+  // items: 16-pixel chunks of rows; a dense window is one row per batch
+  const int64_t row_len = p.dense ? (int64_t)p.w * p.h * p.batch : p.w;
+  const int64_t rows = p.dense ? 1 : (int64_t)p.h * p.batch;
+  const int64_t cpr = (row_len + 15) / 16;
+  const int64_t items = rows * cpr;
+  for (int64_t it = (int64_t)blockIdx.x * HB_T + threadIdx.x; it < items; it += (int64_t)gridDim.x * HB_T) {
+    const int64_t row = it / cpr, chunk = it - row * cpr;
+    const char *base;
+    if (p.dense) {
+      base = p.in + ((int64_t)p.oy * p.pitch + (int64_t)p.ox * p.es);
+    } else {
+      const int b = (int)(row / p.h), y = (int)(row - (int64_t)b * p.h);
+      base = p.in + (int64_t)b * p.bstride + (int64_t)(p.oy + y) * p.pitch + (int64_t)p.ox * p.es;
+    }
+    const T *src = reinterpret_cast<const T *>(base) + chunk * 16;
+    const int64_t left = row_len - chunk * 16;
+    const int n = left < 16 ? (int)left : 16;
+    if (p.vec && n == 16) {
+      constexpr int NV = 16 * sizeof(T) / 16;
+      uint4 v[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) v[k] = ldg16(reinterpret_cast<const char *>(src) + 16 * k);
+      const T *e = reinterpret_cast<const T *>(v);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) put(e[k]);
+    } else {
+      for (int k = 0; k < n; ++k) put(src[k]);
+    }
+  }
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < p.nb; i += HB_T) {
+    const uint32_t c = sb[i];
+    if (c) atomicAdd(&p.bins[i], c);
+  }
+}
+
+}  // namespace
+}  // namespace hgb
+
+using namespace hgb;
+
+extern "C" int hgb_histogram(const hgb_view *in, const hgb_window *win, unsigned num_bins, uint32_t *bins_dev,
+                             uint32_t *bins_host, void *stream) {
+  int rc = check_view(in, "in");
+  if (rc) return rc;
+  HGB_REQUIRE(in->dtype == HGB_U8 || in->dtype == HGB_F32, "hgb_histogram: u8 or f32 pixels expected");
+  HGB_REQUIRE(num_bins >= 1 && num_bins <= kMaxBins, "hgb_histogram: num_bins must be 1..16384");
+  HGB_REQUIRE(bins_dev || bins_host, "hgb_histogram: no result buffer");
+  const hgb_window w = window_or_full(win, *in);
+  rc = check_window(w, *in, "window");
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint32_t *bins = bins_dev;
+  if (!bins) {
+    Workspace ws;
+    rc = workspace_get((size_t)num_bins * 4, &ws);
+    if (rc) return rc;
+    bins = (uint32_t *)ws.base;
+  }
+  HistParams p;
+  memset(&p, 0, sizeof(p));
+  p.in = (const char *)in->data;
+  p.pitch = in->pitch;
+  p.bstride = in->batch_stride;
+  p.ox = w.offset_x;
+  p.oy = w.offset_y;
+  p.w = w.width;
+  p.h = w.height;
+  p.batch = in->batch;
+  p.es = dtype_size(in->dtype);
+  // full-width rows back to back (and whole images back to back in a batch): one flat run
+  p.dense = (w.width == in->width && (int64_t)in->width * p.es == in->pitch &&
+             (in->batch == 1 || (w.height == in->height && in->batch_stride == in->pitch * in->height)))
+                ? 1
+                : 0;
+  const uintptr_t first = (uintptr_t)p.in + (uintptr_t)((int64_t)w.offset_y * p.pitch + (int64_t)w.offset_x * p.es);
+  p.vec = (first % 16 == 0) && (p.dense || (p.pitch % 16 == 0 && (in->batch == 1 || p.bstride % 16 == 0))) ? 1 : 0;
+  p.nb = num_bins;
+  p.bins = bins;
+  const size_t smem = ((size_t)num_bins + (in->dtype == HGB_U8 ? 256 : 0)) * 4;
+  HGB_CHECK_CUDA(cudaMemsetAsync(bins, 0, (size_t)num_bins * 4, st));
+  static bool attr = false;
+  if (!attr) {
+    HGB_CHECK_CUDA(cudaFuncSetAttribute(hist_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)((kMaxBins + 256) * 4)));
+    HGB_CHECK_CUDA(cudaFuncSetAttribute(hist_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(kMaxBins * 4)));
+    attr = true;
+  }
+  const int64_t items = ((int64_t)w.width * w.height * in->batch + 15) / 16;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, in->dtype == HGB_U8 ? (const void *)hist_kernel<uint8_t>
+                                                                                : (const void *)hist_kernel<float>,
+                                                    HB_T, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)num_sms() * per_sm, (items + HB_T - 1) / HB_T));
+  cudaEvent_t ev = before_launch(st);
+  if (in->dtype == HGB_U8)
+    hist_kernel<uint8_t><<<grid, HB_T, smem, st>>>(p);
+  else
+    hist_kernel<float><<<grid, HB_T, smem, st>>>(p);
+  rc = after_launch("hist_kernel", st, ev);
+  if (rc) return rc;
+  if (bins_host) {
+    HGB_CHECK_CUDA(cudaMemcpyAsync(bins_host, bins, (size_t)num_bins * 4, cudaMemcpyDeviceToHost, st));
+    HGB_CHECK_CUDA(cudaStreamSynchronize(st));
+  }
+  return HGB_OK;
+}

@@ -86,8 +86,29 @@ __device__ __forceinline__ void red_release_add(unsigned int *p, unsigned int v)
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Linear-filtering taps of one column (or row) of an L_l tile: the two
+// G_{l+1} indices (tile-relative) and the weights f and 1 - f.
+struct LfTap {
+  int a, c;
+  float f, g;
+};
+
+__device__ __forceinline__ LfTap lf_tap(float s, int x, int n, int origin) {
+  float b = __fmaf_rn(s, (float)x, s * 0.5f) - 0.5f;
+  b = b < 0.0f ? 0.0f : b;
+  const int i = (int)b;
+  const float f = b - (float)i;
+  LfTap t;
+  t.a = min(i, n - 1) - origin;
+  t.c = min(i + 1, n - 1) - origin;
+  t.f = f;
+  t.g = 1.0f - f;
+  return t;
+}
+
 // One 64 x 32 tile of L_level (and the owned part of G_{level+1}).
-__device__ void pyr_tile(const PyrParams &p, const PyrTile t, float *stage, float *gt, bool coherent) {
+__device__ void pyr_tile(const PyrParams &p, const PyrTile t, float *stage, float *gt, LfTap *cols, LfTap *rows,
+                         bool coherent) {
   const LevelMeta A = p.meta[t.img * p.levels + t.level];
   const LevelMeta B = p.meta[t.img * p.levels + t.level + 1];
   const int wl = A.w, hl = A.h, wn = B.w, hn = B.h;
@@ -103,18 +124,30 @@ __device__ void pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
   const int rx0 = nn(Sx, gx0, wl) - 2, rx1 = nn(Sx, gx1 - 1, wl) + 3;
   const int ry0 = nn(Sy, gy0, hl) - 2, ry1 = nn(Sy, gy1 - 1, hl) + 3;
   const int sw = rx1 - rx0, sh = ry1 - ry0;  // <= PY_SW, PY_SH
-  // ---- stage G_l[ry0..ry1) x [rx0..rx1) through the boundary remap
-  for (int c = threadIdx.x; c < sw * sh; c += PY_THREADS) {
-    const int r = c / sw, q = c - r * sw;
-    int y = ry0 + r, x = rx0 + q;
-    float v;
-    const int yy = remap(p.bmode, y, 0, hl), xx = remap(p.bmode, x, 0, wl);
-    if (yy == (int)0x80000000 || xx == (int)0x80000000)
-      v = 0.0f;
-    else
-      v = ld_level(A.g + (int64_t)yy * A.pitch + xx, coherent);
-    stage[r * PY_SW + q] = v;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // ---- stage G_l[ry0..ry1) x [rx0..rx1): a warp per row, lanes along it;
+  // only tiles whose region leaves the level go through the boundary remap
+  const bool inside = rx0 >= 0 && rx1 <= wl && ry0 >= 0 && ry1 <= hl;
+  for (int r = warp; r < sh; r += PY_THREADS / 32) {
+    const int y = ry0 + r;
+    float *dst = stage + r * PY_SW;
+    if (inside) {
+      const float *src = A.g + (int64_t)y * A.pitch + rx0;
+      for (int q = lane; q < sw; q += 32) dst[q] = ld_level(src + q, coherent);
+    } else {
+      const int yy = remap(p.bmode, y, 0, hl);
+      for (int q = lane; q < sw; q += 32) {
+        const int xx = remap(p.bmode, rx0 + q, 0, wl);
+        dst[q] = (yy == (int)0x80000000 || xx == (int)0x80000000) ? 0.0f
+                                                                  : ld_level(A.g + (int64_t)yy * A.pitch + xx, coherent);
+      }
+    }
   }
+  // linear-filtering taps of the tile's columns and rows
+  if (threadIdx.x < PY_TW)
+    cols[threadIdx.x] = lf_tap(sx, t.x0 + threadIdx.x, wn, gx0);
+  else if (threadIdx.x < PY_TW + PY_TH)
+    rows[threadIdx.x - PY_TW] = lf_tap(sy, t.y0 + threadIdx.x - PY_TW, hn, gy0);
   __syncthreads();
   // ---- G_{l+1} on the tile + halo: blur at the nearest-neighbour positions
   const int gw = gx1 - gx0, gh = gy1 - gy0;
@@ -133,39 +166,38 @@ __device__ void pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
       B.g[(int64_t)yp * B.pitch + xp] = acc;
   }
   __syncthreads();
-  // ---- L_l = G_l - LF(G_{l+1})
-  for (int c = threadIdx.x; c < PY_TW * PY_TH; c += PY_THREADS) {
-    const int r = c / PY_TW, q = c - r * PY_TW;
-    const int x = t.x0 + q, y = t.y0 + r;
-    if (x >= wl || y >= hl) continue;
-    float xb = __fmaf_rn(sx, (float)x, sx * 0.5f) - 0.5f;
-    float yb = __fmaf_rn(sy, (float)y, sy * 0.5f) - 0.5f;
-    xb = xb < 0.0f ? 0.0f : xb;
-    yb = yb < 0.0f ? 0.0f : yb;
-    const int xi = (int)xb, yi = (int)yb;
-    const float xf = xb - (float)xi, yf = yb - (float)yi;
-    const int xa = min(xi, wn - 1) - gx0, xc = min(xi + 1, wn - 1) - gx0;
-    const int ya = min(yi, hn - 1) - gy0, yc = min(yi + 1, hn - 1) - gy0;
-    const float wa = __fmul_rn(1.0f - xf, 1.0f - yf), wb = __fmul_rn(xf, 1.0f - yf);
-    const float wc = __fmul_rn(1.0f - xf, yf), wd = __fmul_rn(xf, yf);
-    float lf = __fmul_rn(wa, gt[ya * PY_GW + xa]);
-    lf = __fmaf_rn(wb, gt[ya * PY_GW + xc], lf);
-    lf = __fmaf_rn(wc, gt[yc * PY_GW + xa], lf);
-    lf = __fmaf_rn(wd, gt[yc * PY_GW + xc], lf);
-    const float g = stage[(y - ry0) * PY_SW + (x - rx0)];
-    A.lap[(int64_t)y * A.pitch + x] = __fsub_rn(g, lf);
+  // ---- L_l = G_l - LF(G_{l+1}): a thread per column, rows strided
+  const int tx = threadIdx.x % PY_TW;
+  const int x = t.x0 + tx;
+  if (x < wl) {
+    const LfTap cx = cols[tx];
+    for (int r = threadIdx.x / PY_TW; r < PY_TH; r += PY_THREADS / PY_TW) {
+      const int y = t.y0 + r;
+      if (y >= hl) break;
+      const LfTap cy = rows[r];
+      const float wa = __fmul_rn(cx.g, cy.g), wb = __fmul_rn(cx.f, cy.g);
+      const float wc = __fmul_rn(cx.g, cy.f), wd = __fmul_rn(cx.f, cy.f);
+      float lf = __fmul_rn(wa, gt[cy.a * PY_GW + cx.a]);
+      lf = __fmaf_rn(wb, gt[cy.a * PY_GW + cx.c], lf);
+      lf = __fmaf_rn(wc, gt[cy.c * PY_GW + cx.a], lf);
+      lf = __fmaf_rn(wd, gt[cy.c * PY_GW + cx.c], lf);
+      const float g = stage[(y - ry0) * PY_SW + (x - rx0)];
+      A.lap[(int64_t)y * A.pitch + x] = __fsub_rn(g, lf);
+    }
   }
 }
 
 __global__ void __launch_bounds__(PY_THREADS) pyr_level_kernel(const __grid_constant__ PyrParams p, int first) {
   __shared__ float stage[PY_SW * PY_SH];
   __shared__ float gt[PY_GW * PY_GH];
-  pyr_tile(p, p.tiles[first + blockIdx.x], stage, gt, false);
+  __shared__ LfTap cols[PY_TW], rows[PY_TH];
+  pyr_tile(p, p.tiles[first + blockIdx.x], stage, gt, cols, rows, false);
 }
 
 __global__ void __launch_bounds__(PY_THREADS) pyr_persistent_kernel(const __grid_constant__ PyrParams p) {
   __shared__ float stage[PY_SW * PY_SH];
   __shared__ float gt[PY_GW * PY_GH];
+  __shared__ LfTap cols[PY_TW], rows[PY_TH];
   __shared__ int s_t;
   __shared__ int s_ok;
   for (;;) {
@@ -195,7 +227,7 @@ __global__ void __launch_bounds__(PY_THREADS) pyr_persistent_kernel(const __grid
     const int t = s_t;
     if (t >= p.ntiles) return;
     const PyrTile tl = p.tiles[t];
-    if (s_ok) pyr_tile(p, tl, stage, gt, true);
+    if (s_ok) pyr_tile(p, tl, stage, gt, cols, rows, true);
     __syncthreads();
     if (threadIdx.x == 0) red_release_add(&p.done[tl.img * p.levels + tl.level], 1u);
   }

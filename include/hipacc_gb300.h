@@ -248,6 +248,18 @@ HGB_API int hgb_reduce(const hgb_view *in, const hgb_window *win, int op, void *
 HGB_API int hgb_reduce_noalloc(const hgb_view *in, const hgb_window *win, int op, void *result_dev,
                                void *result_host, void *stream);
 
+/* Binned data (Kernel::binned_data, dsl/kernel.hpp:163-200;
+ * hipaccApplyBinningSegmented, runtime/hipacc_cu.tpp:410-464) of the
+ * histogram binning function (samples-public/2_Global_Operators/Histogram/
+ * src/main.cpp:41-47): for every pixel of the window (of every image of the
+ * batch), bin (unsigned)(pixel / 255.0f * num_bins) += 1.  Indices past the
+ * last bin are dropped (BINNING_CPU_2D, runtime/hipacc_cpu_red.hpp:70-126);
+ * negative or NaN products count in bin 0.  u8 or f32 pixels, num_bins
+ * 1..16384.  `bins_dev` (num_bins uint32, overwritten) and/or `bins_host`
+ * (the call then synchronises the stream). */
+HGB_API int hgb_histogram(const hgb_view *in, const hgb_window *win, unsigned num_bins, uint32_t *bins_dev,
+                          uint32_t *bins_host, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* pyramids (Pyramid / traverse, dsl/pyramid.hpp:97-318;                */
 /* hipaccCreatePyramid, runtime/hipacc_cu.tpp:466-497)                  */

@@ -409,6 +409,32 @@ float orc_reduce_f32(const float *in, int w, int h, long stride, int op, int nth
   return 0.0f;
 }
 
+// ------------------------------------------------------------------ binning
+static inline uint32_t hist_index(float pixel, unsigned num_bins) {
+  const float v = pixel / 255.0f * (float)num_bins;  // two roundings, as the sample
+  if (!(v >= 0.0f)) return 0u;
+  if (v >= 4294967296.0f) return 0xffffffffu;
+  return (uint32_t)v;
+}
+
+void orc_histogram_f32(const float *in, int w, int h, long stride, unsigned num_bins, uint32_t *bins) {
+  for (unsigned i = 0; i < num_bins; ++i) bins[i] = 0;
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      const uint32_t idx = hist_index(in[(long)y * stride + x], num_bins);
+      if (idx < num_bins) bins[idx] += 1u;
+    }
+}
+
+void orc_histogram_u8(const uint8_t *in, int w, int h, long stride, unsigned num_bins, uint32_t *bins) {
+  for (unsigned i = 0; i < num_bins; ++i) bins[i] = 0;
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      const uint32_t idx = hist_index((float)in[(long)y * stride + x], num_bins);
+      if (idx < num_bins) bins[idx] += 1u;
+    }
+}
+
 // Exact-as-possible value of the same reduction (FP64, serial); the error
 // reference for float sums.
 double orc_reduce_f32_exact(const float *in, int w, int h, long stride, int op) {

@@ -76,6 +76,16 @@ uint32_t orc_reduce_max_u8(const uint8_t *in, int w, int h, long stride, int nth
 float    orc_reduce_f32(const float *in, int w, int h, long stride, int op, int nthreads);
 double   orc_reduce_f32_exact(const float *in, int w, int h, long stride, int op);
 
+/* Binning (Kernel::binned_data, dsl/kernel.hpp:163-200; CPU back end
+ * BINNING_CPU_2D, runtime/hipacc_cpu_red.hpp:70-126) with the binning
+ * function of samples-public/2_Global_Operators/Histogram/src/main.cpp:41-47:
+ * bin (unsigned)(pixel / 255.0f * num_bins) += 1; indices >= num_bins are
+ * dropped (the macro's Put).  Negative or NaN products go to bin 0 and
+ * products >= 2^32 to 2^32 - 1 (the saturating conversion; C leaves them
+ * undefined).  u8 pixels are widened to float first.  bins are overwritten. */
+void orc_histogram_f32(const float *in, int w, int h, long stride, unsigned num_bins, uint32_t *bins);
+void orc_histogram_u8(const uint8_t *in, int w, int h, long stride, unsigned num_bins, uint32_t *bins);
+
 /* Bilateral filter (samples-public/3_Preprocessing/Bilateral_Filter/src/main.cpp:63-77)
  * with a float range sigma and float output p/d. */
 void orc_bilateral_f32(const float *in, int w, int h, long stride, float *out, long out_stride,

@@ -29,6 +29,7 @@ f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 
 
 def build(force: bool = False) -> None:
@@ -65,6 +66,8 @@ def lib():
         L.orc_reduce_sum_u8_u64.restype = C.c_uint64
         L.orc_reduce_max_u8.argtypes = [u8p, C.c_int, C.c_int, C.c_long, C.c_int]
         L.orc_reduce_max_u8.restype = C.c_uint32
+        L.orc_histogram_f32.argtypes = [f32p, C.c_int, C.c_int, C.c_long, C.c_uint, u32p]
+        L.orc_histogram_u8.argtypes = [u8p, C.c_int, C.c_int, C.c_long, C.c_uint, u32p]
         L.orc_reduce_f32.argtypes = [f32p, C.c_int, C.c_int, C.c_long, C.c_int, C.c_int]
         L.orc_reduce_f32.restype = C.c_float
         L.orc_reduce_f32_exact.argtypes = [f32p, C.c_int, C.c_int, C.c_long, C.c_int]
@@ -114,6 +117,8 @@ def ref():
             getattr(R, n).argtypes = [f32p, C.c_int, C.c_int]
             getattr(R, n).restype = C.c_float
         R.ref_cpu_red_cores_omp.restype = C.c_int
+        for n in ("ref_cpu_histogram_f32_serial", "ref_cpu_histogram_f32_omp"):
+            getattr(R, n).argtypes = [f32p, C.c_int, C.c_int, C.c_uint, u32p]
         _ref = R
     return _ref
 
@@ -201,6 +206,18 @@ def reduce_sum_u8(img, nthreads=1):
 def reduce_max_u8(img, nthreads=1):
     img = np.ascontiguousarray(img, np.uint8)
     return int(lib().orc_reduce_max_u8(img, img.shape[1], img.shape[0], img.shape[1], nthreads))
+
+
+def histogram(img, num_bins):
+    """Binned data of the histogram sample's binning function (u32 bins)."""
+    bins = np.zeros(num_bins, np.uint32)
+    if img.dtype == np.uint8:
+        img = np.ascontiguousarray(img)
+        lib().orc_histogram_u8(img, img.shape[1], img.shape[0], img.shape[1], num_bins, bins)
+    else:
+        img = np.ascontiguousarray(img, np.float32)
+        lib().orc_histogram_f32(img, img.shape[1], img.shape[0], img.shape[1], num_bins, bins)
+    return bins
 
 
 def reduce_f32(img, op=SUM, nthreads=1):

@@ -101,6 +101,14 @@ def main():
     out["pyramid_gauss"] = go
     out["pyramid_lap"] = lo
     path = os.path.join(HERE, "hipacc_ref_golden.npz")
+    # binning: the histogram sample's binning function through BINNING_CPU_2D
+    hist = (rng.random((29, 41)) * 255.0).astype(np.float32)
+    hist[0, :3] = [255.0, 0.0, 254.999]
+    out["hist_in"] = hist
+    for nb in (7, 64, 256, 1000):
+        bins = np.zeros(nb, np.uint32)
+        R.ref_cpu_histogram_f32_serial(hist, 41, 29, nb, bins)
+        out[f"hist_{nb}"] = bins
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path), "bytes,", len(out), "arrays")
 

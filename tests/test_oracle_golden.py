@@ -44,6 +44,17 @@ def test_sobel_gray_reduce_golden(oracle, golden):
     assert np.float32(O.reduce_f32(f, O.SUM, 1)) == golden["red_f32_cpu2d_serial"][0]
 
 
+def test_histogram_golden(oracle, golden):
+    """Binning: the restated histogram against the reference's BINNING_CPU_2D
+    with the histogram sample's binning function (255.0 lands past the last
+    bin and is dropped)."""
+    img = golden["hist_in"]
+    for nb in (7, 64, 256, 1000):
+        assert np.array_equal(oracle.histogram(img, nb), golden[f"hist_{nb}"])
+    u8 = img.astype(np.uint8)
+    assert np.array_equal(oracle.histogram(u8, 256), oracle.histogram(u8.astype(np.float32), 256))
+
+
 def test_bilateral_golden(oracle, golden):
     O = oracle
     for size in (5, 13):
