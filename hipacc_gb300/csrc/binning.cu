@@ -9,12 +9,15 @@
 // indices past the last bin.  The float-to-unsigned conversion here saturates
 // (negative and NaN products land in bin 0), where C leaves it undefined.
 //
-// GB300 form: one resident wave of CTAs, each with a private histogram in
-// shared memory (shared-memory atomics), the image read as 16-pixel chunks
+// GB300 form: one resident wave of CTAs, each with private histograms in
+// shared memory updated by shared-memory atomics -- for u8 pixels and up to
+// 256 bins one column per lane (a warp's 32 updates land in 32 banks),
+// otherwise one copy per warp up to 1024 bins and one copy beyond -- the
+// image read as 16-pixel chunks
 // with 16-byte loads where the layout allows, and one global atomic add per
 // non-empty private bin at the end.  Integer sums, so the result does not
 // depend on the order.  u8 pixels map through a 256-entry table computed
-// with the same float arithmetic.
+// with the same float arithmetic, replicated once per shared-memory bank.
 #include <algorithm>
 
 #include "hgb_internal.cuh"
@@ -33,6 +36,7 @@ struct HistParams {
   int dense;   // window rows back to back over the batch: one flat run
   int vec;     // 16-byte loads legal for every chunk
   unsigned nb;
+  int layout;  // private histograms per CTA: 0 one, 1 one per warp, 2 one column per lane
   uint32_t *bins;
 };
 
@@ -44,19 +48,26 @@ __device__ __forceinline__ uint32_t bin_of(float px, unsigned nb) {
 template <typename T>
 __global__ void __launch_bounds__(HB_T) hist_kernel(const __grid_constant__ HistParams p) {
   extern __shared__ uint32_t hist_smem[];
-  uint32_t *sb = hist_smem;
-  uint32_t *lut = hist_smem + p.nb;  // u8 only
-  for (unsigned i = threadIdx.x; i < p.nb; i += HB_T) sb[i] = 0u;
+  const unsigned copies = p.layout == 2 ? 32u : (p.layout == 1 ? (unsigned)(HB_T / 32) : 1u);
+  const unsigned nall = p.nb * copies;
+  // u8 only: the value -> bin table, one copy per bank (entry v of lane l at
+  // v * 32 + l), so a warp's 32 lookups never conflict
+  uint32_t *lut = hist_smem + nall;
+  for (unsigned i = threadIdx.x; i < nall; i += HB_T) hist_smem[i] = 0u;
+  // lane columns: bin i of lane l at i * 32 + l, so a warp's 32 updates hit 32
+  // banks; per-warp copies: warps do not contend on a bin
+  const unsigned lane = threadIdx.x & 31;
+  uint32_t *sb = hist_smem + (p.layout == 1 ? (threadIdx.x >> 5) * p.nb : 0u);
   if constexpr (sizeof(T) == 1)
-    for (int v = threadIdx.x; v < 256; v += HB_T) lut[v] = bin_of((float)v, p.nb);
+    for (int i = threadIdx.x; i < 256 * 32; i += HB_T) lut[i] = bin_of((float)(i >> 5), p.nb);
   __syncthreads();
   auto put = [&](T px) {
     uint32_t idx;
     if constexpr (sizeof(T) == 1)
-      idx = lut[(uint32_t)px];
+      idx = lut[((uint32_t)px << 5) | (threadIdx.x & 31)];
     else
       idx = bin_of((float)px, p.nb);
-    if (idx < p.nb) atomicAdd(&sb[idx], 1u);
+    if (idx < p.nb) atomicAdd(&sb[p.layout == 2 ? (idx << 5) | lane : idx], 1u);
   };
   // items: 16-pixel chunks of rows; a dense window is one row per batch
   const int64_t row_len = p.dense ? (int64_t)p.w * p.h * p.batch : p.w;
@@ -89,7 +100,11 @@ __global__ void __launch_bounds__(HB_T) hist_kernel(const __grid_constant__ Hist
   }
   __syncthreads();
   for (unsigned i = threadIdx.x; i < p.nb; i += HB_T) {
-    const uint32_t c = sb[i];
+    uint32_t c = 0;
+    if (p.layout == 2)
+      for (int k = 0; k < 32; ++k) c += hist_smem[(i << 5) | ((k + i) & 31)];  // rotate to spread banks
+    else
+      for (unsigned k = 0; k < copies; ++k) c += hist_smem[k * p.nb + i];
     if (c) atomicAdd(&p.bins[i], c);
   }
 }
@@ -136,13 +151,16 @@ extern "C" int hgb_histogram(const hgb_view *in, const hgb_window *win, unsigned
   const uintptr_t first = (uintptr_t)p.in + (uintptr_t)((int64_t)w.offset_y * p.pitch + (int64_t)w.offset_x * p.es);
   p.vec = (first % 16 == 0) && (p.dense || (p.pitch % 16 == 0 && (in->batch == 1 || p.bstride % 16 == 0))) ? 1 : 0;
   p.nb = num_bins;
+  // measured on 4096^2 images: lane columns help u8 (23.0 vs 24.8 us), per-warp copies f32 (24.8 vs 37 us)
+  p.layout = (in->dtype == HGB_U8 && num_bins <= 256) ? 2 : (num_bins <= 1024 ? 1 : 0);
   p.bins = bins;
-  const size_t smem = ((size_t)num_bins + (in->dtype == HGB_U8 ? 256 : 0)) * 4;
+  const size_t copies = p.layout == 2 ? 32 : (p.layout == 1 ? HB_T / 32 : 1);
+  const size_t smem = ((size_t)num_bins * copies + (in->dtype == HGB_U8 ? 256 * 32 : 0)) * 4;
   HGB_CHECK_CUDA(cudaMemsetAsync(bins, 0, (size_t)num_bins * 4, st));
   static bool attr = false;
   if (!attr) {
     HGB_CHECK_CUDA(cudaFuncSetAttribute(hist_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)((kMaxBins + 256) * 4)));
+                                        (int)((kMaxBins + 256 * 32) * 4)));
     HGB_CHECK_CUDA(cudaFuncSetAttribute(hist_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(kMaxBins * 4)));
     attr = true;

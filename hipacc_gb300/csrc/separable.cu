@@ -18,11 +18,13 @@
 //
 // GB300 form: a TMA-legal image (16-byte aligned base, pitch and batch
 // stride) is staged by one cp.async.bulk.tensor load per CTA in its storage
-// type (bf16 / f16 tiles are then widened to FP32 in shared memory); cells
-// outside the image, which TMA fills with zeros, are patched with the boundary
-// rule.  Other layouts stage with 16-byte global loads.  Both passes run
-// packed f32x2 fused multiply-adds on pairs of adjacent outputs, keeping each
-// output's tap order.
+// type, and the row pass widens bf16 / f16 as it reads (half the shared memory
+// of an FP32 tile, so more CTAs per SM); cells outside the image, which TMA
+// fills with zeros, are patched with the boundary rule (a CONSTANT cell holds
+// the constant in the storage type).  Other layouts stage an FP32 tile with
+// 16-byte global loads.  Both passes run packed f32x2 fused multiply-adds on
+// pairs of adjacent outputs, keeping each output's tap order.
+#include <algorithm>
 #include <type_traits>
 
 #include "stage.cuh"
@@ -59,10 +61,75 @@ struct SepShape {
   static constexpr int HL = round_up(R, VI);
   static constexpr int SW = HL + SP_TW + round_up(R, VI);
   static constexpr int SH = SP_TH + K - 1;
-  // raw storage-type tile (TMA destination; bf16 / f16 only), FP32 tile, row-pass buffer
-  static constexpr size_t raw = std::is_same<T, float>::value ? 0 : (((size_t)SH * SW * sizeof(T) + 127) / 128 * 128);
-  static constexpr size_t smem = raw + sizeof(float) * ((size_t)SH * SW + (size_t)SH * SP_TW) + 128;
+  // staged tile: the storage type when TMA stages it, FP32 otherwise; then the row-pass buffer
+  static constexpr size_t tile_tma = ((size_t)SH * SW * sizeof(T) + 127) / 128 * 128;
+  static constexpr size_t tile_ldg = ((size_t)SH * SW * sizeof(float) + 127) / 128 * 128;
+  static constexpr size_t rowbuf = sizeof(float) * (size_t)SH * SP_TW;
+  static constexpr size_t smem_tma = tile_tma + rowbuf + 128;
+  static constexpr size_t smem_ldg = tile_ldg + rowbuf + 128;
 };
+
+// four consecutive staged values as floats (the tile holds the storage type
+// or FP32)
+template <typename TT>
+__device__ __forceinline__ float4 load4(const TT *p) {
+  if constexpr (std::is_same<TT, float>::value) {
+    return *reinterpret_cast<const float4 *>(p);
+  } else {
+    const uint2 u = *reinterpret_cast<const uint2 *>(p);
+    float f[8];
+    Vec16<TT>::unpack(make_uint4(u.x, u.y, 0u, 0u), f);
+    return make_float4(f[0], f[1], f[2], f[3]);
+  }
+}
+
+// row pass over a staged tile: 4 outputs per thread per staged row into the
+// FP32 row buffer
+template <typename TT, int K, int SW, int SH, int HL>
+__device__ __forceinline__ void row_pass(const SepParams &p, const TT *tile, float *rowb, int j0, int tx, int ty) {
+  constexpr int R = K / 2;
+  constexpr int OFF = (HL - R) % 4;
+  constexpr int NV = cdiv(OFF + SP_PX + K - 1, 4);
+  const int cb = HL - R - OFF + tx * SP_PX;
+  for (int r = ty; r < SH; r += SP_BY) {
+    float win[NV * 4];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const float4 t = load4(&tile[r * SW + cb + 4 * v]);
+      win[4 * v] = t.x;
+      win[4 * v + 1] = t.y;
+      win[4 * v + 2] = t.z;
+      win[4 * v + 3] = t.w;
+    }
+    f2 E[NV * 2], O[NV * 2];
+#pragma unroll
+    for (int j = 0; j < NV * 2; ++j) {
+      E[j] = f2_pack(win[2 * j], win[2 * j + 1]);
+      O[j] = f2_pack(win[2 * j + 1], 2 * j + 2 < NV * 4 ? win[2 * j + 2] : 0.0f);
+    }
+    f2 a2[SP_PX / 2];
+#pragma unroll
+    for (int pp = 0; pp < SP_PX / 2; ++pp) {
+      a2[pp] = 0ull;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int st = OFF + 2 * pp + k;
+        a2[pp] = f2_fma(p.row2[k], (st & 1) ? O[st >> 1] : E[st >> 1], a2[pp]);
+      }
+    }
+    float acc[SP_PX];
+#pragma unroll
+    for (int pp = 0; pp < SP_PX / 2; ++pp) {
+      acc[2 * pp] = f2_lo(a2[pp]);
+      acc[2 * pp + 1] = f2_hi(a2[pp]);
+    }
+    const int ay = j0 - R + r;
+    if (p.bmode == HGB_BOUNDARY_CONSTANT && (ay < 0 || ay >= p.h))
+#pragma unroll
+      for (int px = 0; px < SP_PX; ++px) acc[px] = p.cval;
+    *reinterpret_cast<float4 *>(&rowb[r * SP_TW + tx * SP_PX]) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+  }
+}
 
 template <typename T, int K>
 __global__ void __launch_bounds__(SP_BX *SP_BY) separable_kernel(const __grid_constant__ SepParams p) {
@@ -72,19 +139,21 @@ __global__ void __launch_bounds__(SP_BX *SP_BY) separable_kernel(const __grid_co
   extern __shared__ __align__(128) uint8_t sep_dsm[];
   __shared__ __align__(8) uint64_t bar;
   uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(sep_dsm) + 127) & ~(uintptr_t)127);
-  T *raw = reinterpret_cast<T *>(base);
-  float *tile = reinterpret_cast<float *>(base + S::raw);
-  float *rowb = tile + SH * SW;
   const int b = blockIdx.z;
   const int i0 = blockIdx.x * SP_TW, j0 = blockIdx.y * SP_TH;
   const int X0 = i0 - HL, Y0 = j0 - R;
   const char *img = p.in + (int64_t)b * p.in_bstride;
+  const int tx = threadIdx.x % SP_BX, ty = threadIdx.x / SP_BX;
+  float *rowb;
   if (p.use_tma) {
+    // the tile stays in the storage type; the row pass widens as it reads
+    T *tile = reinterpret_cast<T *>(base);
+    rowb = reinterpret_cast<float *>(base + S::tile_tma);
     if (threadIdx.x == 0) {
       mbar_init(&bar, 1);
       mbar_fence_init();
       mbar_expect_tx(&bar, SH * SW * (int)sizeof(T));
-      tma_load_3d(std::is_same<T, float>::value ? (void *)tile : (void *)raw, &p.map, X0, Y0, b, &bar);
+      tma_load_3d(tile, &p.map, X0, Y0, b, &bar);
     }
     __syncthreads();
     if (!mbar_wait(&bar, 0)) {
@@ -94,19 +163,9 @@ __global__ void __launch_bounds__(SP_BX *SP_BY) separable_kernel(const __grid_co
       }
       return;
     }
-    if constexpr (!std::is_same<T, float>::value) {
-      // widen the staged tile to FP32, 8 elements per 16-byte chunk
-      constexpr int NCH = SH * SW / 8;
-      for (int c = threadIdx.x; c < NCH; c += NT) {
-        float f[8];
-        Vec16<T>::unpack(reinterpret_cast<const uint4 *>(raw)[c], f);
-        *reinterpret_cast<float4 *>(&tile[8 * c]) = make_float4(f[0], f[1], f[2], f[3]);
-        *reinterpret_cast<float4 *>(&tile[8 * c + 4]) = make_float4(f[4], f[5], f[6], f[7]);
-      }
-    }
     if (X0 < 0 || X0 + SW > p.w || Y0 < 0 || Y0 + SH > p.h) {
-      if constexpr (!std::is_same<T, float>::value) __syncthreads();
-      // cells outside the image (zero-filled by TMA): left / right columns, top / bottom rows
+      // cells outside the image (zero-filled by TMA): left / right columns,
+      // top / bottom rows; CONSTANT cells take the constant in the storage type
       const int nl = max(0, min(SW, -X0)), rs = max(0, min(SW, p.w - X0));
       const int nt = max(0, min(SH, -Y0)), bs = max(0, min(SH, p.h - Y0));
       const int ncl = nl * SH, ncr = (SW - rs) * SH, nrt = nt * SW, nrb = (SH - bs) * SW;
@@ -131,58 +190,18 @@ __global__ void __launch_bounds__(SP_BX *SP_BY) separable_kernel(const __grid_co
         }
         const int ry = remap(p.bmode, Y0 + r, 0, p.h), rx = remap(p.bmode, X0 + q, 0, p.w);
         tile[r * SW + q] = (ry == (int)0x80000000 || rx == (int)0x80000000)
-                               ? p.cval
-                               : Storage<T>::load(reinterpret_cast<const T *>(img + (int64_t)ry * p.in_pitch) + rx);
+                               ? Storage<T>::from_f(p.cval)
+                               : reinterpret_cast<const T *>(img + (int64_t)ry * p.in_pitch)[rx];
       }
     }
+    __syncthreads();
+    row_pass<T, K, SW, SH, HL>(p, tile, rowb, j0, tx, ty);
   } else {
+    float *tile = reinterpret_cast<float *>(base);
+    rowb = reinterpret_cast<float *>(base + S::tile_ldg);
     stage_tile<T, SW, SH, NT>(tile, img, p.in_pitch, X0, Y0, 0, p.w, 0, p.h, p.bmode, p.cval, p.vec_in);
-  }
-  __syncthreads();
-  const int tx = threadIdx.x % SP_BX, ty = threadIdx.x / SP_BX;
-  // ---- row pass: 4 outputs per thread per staged row
-  {
-    constexpr int OFF = (HL - R) % 4;
-    constexpr int NV = cdiv(OFF + SP_PX + K - 1, 4);
-    const int cb = HL - R - OFF + tx * SP_PX;
-    for (int r = ty; r < SH; r += SP_BY) {
-      float win[NV * 4];
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        const float4 t = *reinterpret_cast<const float4 *>(&tile[r * SW + cb + 4 * v]);
-        win[4 * v] = t.x;
-        win[4 * v + 1] = t.y;
-        win[4 * v + 2] = t.z;
-        win[4 * v + 3] = t.w;
-      }
-      f2 E[NV * 2], O[NV * 2];
-#pragma unroll
-      for (int j = 0; j < NV * 2; ++j) {
-        E[j] = f2_pack(win[2 * j], win[2 * j + 1]);
-        O[j] = f2_pack(win[2 * j + 1], 2 * j + 2 < NV * 4 ? win[2 * j + 2] : 0.0f);
-      }
-      f2 a2[SP_PX / 2];
-#pragma unroll
-      for (int pp = 0; pp < SP_PX / 2; ++pp) {
-        a2[pp] = 0ull;
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-          const int st = OFF + 2 * pp + k;
-          a2[pp] = f2_fma(p.row2[k], (st & 1) ? O[st >> 1] : E[st >> 1], a2[pp]);
-        }
-      }
-      float acc[SP_PX];
-#pragma unroll
-      for (int pp = 0; pp < SP_PX / 2; ++pp) {
-        acc[2 * pp] = f2_lo(a2[pp]);
-        acc[2 * pp + 1] = f2_hi(a2[pp]);
-      }
-      const int ay = j0 - R + r;
-      if (p.bmode == HGB_BOUNDARY_CONSTANT && (ay < 0 || ay >= p.h))
-#pragma unroll
-        for (int px = 0; px < SP_PX; ++px) acc[px] = p.cval;
-      *reinterpret_cast<float4 *>(&rowb[r * SP_TW + tx * SP_PX]) = make_float4(acc[0], acc[1], acc[2], acc[3]);
-    }
+    __syncthreads();
+    row_pass<float, K, SW, SH, HL>(p, tile, rowb, j0, tx, ty);
   }
   __syncthreads();
   // ---- column pass: 4 x 4 outputs per thread
@@ -231,7 +250,6 @@ constexpr CUtensorMapDataType tma_dtype() {
 template <typename T, int K>
 int launch_sep_k(const SepParams &p0, int batch, cudaStream_t st) {
   using S = SepShape<T, K>;
-  constexpr size_t smem = S::smem;
   SepParams p = p0;
   p.use_tma = 0;
   if (tma_legal(p.in, p.in_pitch, p.in_bstride, batch) &&
@@ -242,9 +260,11 @@ int launch_sep_k(const SepParams &p0, int batch, cudaStream_t st) {
   }
   static bool attr = false;
   if (!attr) {
-    HGB_CHECK_CUDA(cudaFuncSetAttribute(separable_kernel<T, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    HGB_CHECK_CUDA(cudaFuncSetAttribute(separable_kernel<T, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)std::max(S::smem_tma, S::smem_ldg)));
     attr = true;
   }
+  const size_t smem = p.use_tma ? S::smem_tma : S::smem_ldg;
   dim3 grid(cdiv(p.w, SP_TW), cdiv(p.h, SP_TH), batch);
   cudaEvent_t ev = before_launch(st);
   separable_kernel<T, K><<<grid, SP_BX * SP_BY, smem, st>>>(p);
