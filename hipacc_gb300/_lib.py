@@ -63,6 +63,14 @@ SIGNATURES = {
     "hgb_image_read": (i32, [vp, vp, vp]),
     "hgb_image_read_async": (i32, [vp, vp, vp]),
     "hgb_histogram": (i32, [vp, vp, C.c_uint, vp, vp, vp]),
+    "hgb_stream_create": (i32, [vp]),
+    "hgb_stream_destroy": (i32, [vp]),
+    "hgb_stream_synchronize": (i32, [vp]),
+    "hgb_stream_wait": (i32, [vp, vp]),
+    "hgb_graph_begin": (i32, [vp]),
+    "hgb_graph_end": (i32, [vp, vp]),
+    "hgb_graph_launch": (i32, [vp, vp]),
+    "hgb_graph_destroy": (i32, [vp]),
     "hgb_image_copy": (i32, [vp, vp, vp]),
     "hgb_image_copy_region": (i32, [vp, WP, vp, WP, vp]),
     "hgb_local_op": (i32, [VP, WP, VP, WP, vp, vp, vp, i32, i32, i32, i32, f32, vp]),

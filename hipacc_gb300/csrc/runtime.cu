@@ -261,6 +261,65 @@ int hgb_image_read_async(const hgb_image *img, void *host, void *stream) {
   return HGB_OK;
 }
 
+int hgb_stream_create(void **stream) {
+  HGB_REQUIRE(stream, "hgb_stream_create: null argument");
+  cudaStream_t s = nullptr;
+  HGB_CHECK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *stream = s;
+  return HGB_OK;
+}
+
+int hgb_stream_destroy(void *stream) {
+  if (!stream) return HGB_OK;
+  HGB_CHECK_CUDA(cudaStreamDestroy((cudaStream_t)stream));
+  return HGB_OK;
+}
+
+int hgb_stream_synchronize(void *stream) {
+  HGB_CHECK_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return HGB_OK;
+}
+
+int hgb_stream_wait(void *waiter, void *signaller) {
+  cudaEvent_t e = nullptr;
+  HGB_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaError_t err = cudaEventRecord(e, (cudaStream_t)signaller);
+  if (err == cudaSuccess) err = cudaStreamWaitEvent((cudaStream_t)waiter, e, 0);
+  cudaEventDestroy(e);  // released once the recorded work completes
+  if (err != cudaSuccess) return cuda_error(err, "hgb_stream_wait");
+  return HGB_OK;
+}
+
+int hgb_graph_begin(void *stream) {
+  HGB_REQUIRE(stream, "hgb_graph_begin: the legacy default stream cannot be recorded");
+  HGB_CHECK_CUDA(cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal));
+  return HGB_OK;
+}
+
+int hgb_graph_end(void *stream, hgb_graph **out) {
+  HGB_REQUIRE(stream && out, "hgb_graph_end: null argument");
+  cudaGraph_t g = nullptr;
+  HGB_CHECK_CUDA(cudaStreamEndCapture((cudaStream_t)stream, &g));
+  cudaGraphExec_t x = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&x, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_error(e, "hgb_graph_end: instantiate");
+  *out = reinterpret_cast<hgb_graph *>(x);
+  return HGB_OK;
+}
+
+int hgb_graph_launch(const hgb_graph *graph, void *stream) {
+  HGB_REQUIRE(graph, "hgb_graph_launch: null graph");
+  HGB_CHECK_CUDA(cudaGraphLaunch((cudaGraphExec_t)graph, (cudaStream_t)stream));
+  return HGB_OK;
+}
+
+int hgb_graph_destroy(hgb_graph *graph) {
+  if (!graph) return HGB_OK;
+  HGB_CHECK_CUDA(cudaGraphExecDestroy((cudaGraphExec_t)graph));
+  return HGB_OK;
+}
+
 int hgb_image_copy(const hgb_image *src, hgb_image *dst, void *stream) {
   HGB_REQUIRE(src && dst, "hgb_image_copy: null argument");
   HGB_REQUIRE(src->view.width == dst->view.width && src->view.height == dst->view.height &&

@@ -151,6 +151,25 @@ HGB_API int hgb_image_copy(const hgb_image *src, hgb_image *dst, void *stream);
 HGB_API int hgb_image_copy_region(const hgb_image *src, const hgb_window *src_win, hgb_image *dst,
                           const hgb_window *dst_win, void *stream);
 
+/* Streams and whole-program graphs: the CUDA-graph mode of Hipacc's generated
+ * host code (hipaccLaunchKernelCudaGraph, runtime/hipacc_cu_standalone.hpp:331-356;
+ * graph assembly in lib/Rewrite/Rewrite.cpp:423-477).  Calls issued on a stream
+ * between hgb_graph_begin and hgb_graph_end are recorded, not run; the graph
+ * replays them with one launch.  Independent branches are expressed with
+ * hgb_stream_wait: `waiter` waits for the work queued so far on `signaller`
+ * (a fork or a join edge).  Calls that synchronise (host results, image
+ * read-back) or allocate (hgb_image_create, the first growth of the workspace:
+ * call hgb_workspace_reserve first) cannot be recorded. */
+HGB_API int hgb_stream_create(void **stream);
+HGB_API int hgb_stream_destroy(void *stream);
+HGB_API int hgb_stream_synchronize(void *stream);
+HGB_API int hgb_stream_wait(void *waiter, void *signaller);
+typedef struct hgb_graph hgb_graph;
+HGB_API int hgb_graph_begin(void *stream);
+HGB_API int hgb_graph_end(void *stream, hgb_graph **out);
+HGB_API int hgb_graph_launch(const hgb_graph *graph, void *stream);
+HGB_API int hgb_graph_destroy(hgb_graph *graph);
+
 /* ------------------------------------------------------------------ */
 /* local operators                                                     */
 /* ------------------------------------------------------------------ */

@@ -70,6 +70,65 @@ inline std::string hipaccInitCUDA(int device = 0) {
 inline void hipaccEnableTiming(bool on) { check(hgb_set_timing(on ? 1 : 0), "hipaccEnableTiming"); }
 inline float hipacc_last_kernel_timing() { return hgb_last_kernel_timing(); }
 
+// The stream every call below is queued on (the stream of an
+// ExecutionParameter, runtime/hipacc_cu_standalone.hpp:293-295); nullptr is
+// the legacy default stream.  Per thread.
+inline void *&current_stream() {
+  static thread_local void *s = nullptr;
+  return s;
+}
+inline void hipaccSetStream(void *stream) { current_stream() = stream; }
+
+// A stream owned by the library (for hosts compiled without the CUDA headers).
+class Stream {
+ public:
+  Stream() { check(hgb_stream_create(&s_), "hgb_stream_create"); }
+  ~Stream() { hgb_stream_destroy(s_); }
+  Stream(const Stream &) = delete;
+  Stream &operator=(const Stream &) = delete;
+  void *get() const { return s_; }
+  void synchronize() const { check(hgb_stream_synchronize(s_), "hgb_stream_synchronize"); }
+  // this stream waits for the work queued so far on `other` (fork / join)
+  void wait(const Stream &other) const { check(hgb_stream_wait(s_, other.s_), "hgb_stream_wait"); }
+
+ private:
+  void *s_ = nullptr;
+};
+
+// Whole-program graph (Hipacc's CUDA-graph mode, hipaccLaunchKernelCudaGraph,
+// runtime/hipacc_cu_standalone.hpp:331-356): between begin() and end() the
+// kernels executed on this thread are recorded on the graph's stream instead of
+// running; launch() replays them all with one launch.  Only device work can be
+// recorded: read images back (Image::data(), reduced_data()) after launch().
+class CudaGraph {
+ public:
+  CudaGraph() = default;
+  ~CudaGraph() { hgb_graph_destroy(g_); }
+  CudaGraph(const CudaGraph &) = delete;
+  CudaGraph &operator=(const CudaGraph &) = delete;
+  void begin() {
+    saved_ = current_stream();
+    current_stream() = stream_.get();
+    check(hgb_graph_begin(stream_.get()), "CudaGraph::begin");
+  }
+  void end() {
+    hgb_graph *g = nullptr;
+    const int st = hgb_graph_end(stream_.get(), &g);
+    current_stream() = saved_;
+    check(st, "CudaGraph::end");
+    hgb_graph_destroy(g_);
+    g_ = g;
+  }
+  void launch() { check(hgb_graph_launch(g_, stream_.get()), "CudaGraph::launch"); }
+  void synchronize() { stream_.synchronize(); }
+  Stream &stream() { return stream_; }
+
+ private:
+  Stream stream_;
+  hgb_graph *g_ = nullptr;
+  void *saved_ = nullptr;
+};
+
 template <typename T> struct dtype_of;
 template <> struct dtype_of<uchar> { static constexpr int value = HGB_U8; };
 template <> struct dtype_of<uchar4> { static constexpr int value = HGB_U8X4; };
@@ -97,12 +156,12 @@ class Image {
   int height() const { return h_; }
   // hipaccReadMemory: refresh the host mirror and return it
   T *data() {
-    check(hgb_image_read(img_.get(), host_.data(), nullptr), "hipaccReadMemory");
+    check(hgb_image_read(img_.get(), host_.data(), current_stream()), "hipaccReadMemory");
     return host_.data();
   }
   // hipaccWriteMemory
   Image &operator=(const T *other) {
-    check(hgb_image_write(img_.get(), other, nullptr), "hipaccWriteMemory");
+    check(hgb_image_write(img_.get(), other, current_stream()), "hipaccWriteMemory");
     std::memcpy(host_.data(), other, sizeof(T) * host_.size());
     return *this;
   }
@@ -135,7 +194,7 @@ inline T *hipaccReadMemory(const std::shared_ptr<Image<T>> &img) {
 }
 template <typename T>
 inline void hipaccCopyMemory(const std::shared_ptr<Image<T>> &src, std::shared_ptr<Image<T>> &dst) {
-  check(hgb_image_copy(src->handle(), dst->handle(), nullptr), "hipaccCopyMemory");
+  check(hgb_image_copy(src->handle(), dst->handle(), current_stream()), "hipaccCopyMemory");
 }
 
 // ---------------------------------------------------------------- masks
@@ -276,7 +335,7 @@ template <typename T>
 inline T reduce_image(const Image<T> &img, const hgb_window &win, Reduce op) {
   hgb_view v = img.view();
   unsigned char raw[8];
-  check(hgb_reduce(&v, &win, (int)op, nullptr, raw, nullptr), "reduced_data");
+  check(hgb_reduce(&v, &win, (int)op, nullptr, raw, current_stream()), "reduced_data");
   if (std::is_floating_point<T>::value) {
     double d;
     std::memcpy(&d, raw, 8);
@@ -298,7 +357,7 @@ class Convolution : public Kernel<T> {
   void launch() override {
     hgb_view iv = in_.image().view(), ov = this->out_view();
     check(hgb_local_op(&iv, &in_.window(), &ov, this->out_window(), m_.coefficients(), nullptr, nullptr, m_.size_x(),
-                       m_.size_y(), (int)mode_, (int)in_.mode(), (float)in_.constant(), nullptr),
+                       m_.size_y(), (int)mode_, (int)in_.mode(), (float)in_.constant(), current_stream()),
           "Convolution::execute");
   }
   Accessor<T> &in_;
@@ -316,7 +375,7 @@ class DomainReduce : public Kernel<T> {
   void launch() override {
     hgb_view iv = in_.image().view(), ov = this->out_view();
     check(hgb_local_op(&iv, &in_.window(), &ov, this->out_window(), nullptr, nullptr, d_.domain(), d_.size_x(),
-                       d_.size_y(), (int)mode_, (int)in_.mode(), (float)in_.constant(), nullptr),
+                       d_.size_y(), (int)mode_, (int)in_.mode(), (float)in_.constant(), current_stream()),
           "DomainReduce::execute");
   }
   Accessor<T> &in_;
@@ -334,7 +393,7 @@ class Separable : public Kernel<T> {
   void launch() override {
     hgb_view iv = in_.image().view(), ov = this->out_view();
     check(hgb_separable(&iv, &ov, row_.data(), col_.data(), (int)row_.size(), (int)in_.mode(), (float)in_.constant(),
-                        nullptr),
+                        current_stream()),
           "Separable::execute");
   }
   Accessor<T> &in_;
@@ -351,7 +410,7 @@ class BilateralFilter : public Kernel<T> {
   void launch() override {
     hgb_view iv = in_.image().view(), ov = this->out_view();
     check(hgb_bilateral(&iv, &ov, m_.coefficients(), m_.size_x(), sigma_r_, (int)in_.mode(), (float)in_.constant(), 0,
-                        nullptr),
+                        current_stream()),
           "BilateralFilter::execute");
   }
   Accessor<T> &in_;
@@ -364,37 +423,48 @@ class BilateralFilter : public Kernel<T> {
 class SobelMagnitude : public Kernel<uchar> {
  public:
   SobelMagnitude(IterationSpace<uchar> &it, Accessor<uchar> &in, Mask<int> &mx, Mask<int> &my)
-      : Kernel<uchar>(it), in_(in), mx_(mx), my_(my) {}
+      : Kernel<uchar>(it), in_(in), mx_(mx), my_(my) {
+    // device slots of the fused sum and max (created here, so execute() allocates nothing)
+    hgb_image *d = nullptr;
+    check(hgb_image_create(HGB_U64, 2, 1, 256, nullptr, &d), "SobelMagnitude scratch");
+    scratch_.reset(d, [](hgb_image *p) { hgb_image_destroy(p); });
+  }
   unsigned long long reduced_sum() {
-    execute();
+    fetch();
     return host_[0];
   }
   uchar reduced_max() {
-    execute();
+    fetch();
     return (uchar)host_[1];
   }
 
  protected:
   void launch() override {
-    hgb_view iv = in_.image().view(), ov = this->out_view();
-    void *d = nullptr;
-    check(hgb_image_create(HGB_U64, 2, 1, 256, nullptr, reinterpret_cast<hgb_image **>(&d)), "SobelMagnitude scratch");
-    hgb_view sv;
-    hgb_image_get_view(reinterpret_cast<hgb_image *>(d), &sv);
+    hgb_view iv = in_.image().view(), ov = this->out_view(), sv;
+    hgb_image_get_view(scratch_.get(), &sv);
     uint64_t *sum = (uint64_t *)sv.data;
     uint32_t *mx = (uint32_t *)((char *)sv.data + 8);
-    int st = hgb_sobel_mag(&iv, &ov, mx_.coefficients(), my_.coefficients(), mx_.size_x(), (int)in_.mode(),
-                           (int)in_.constant(), sum, mx, nullptr);
-    if (st == HGB_OK) {
-      unsigned long long tmp[2] = {0, 0};
-      st = hgb_image_read(reinterpret_cast<hgb_image *>(d), tmp, nullptr);
-      host_[0] = tmp[0];
-      host_[1] = tmp[1] & 0xffffffffull;
-    }
-    hgb_image_destroy(reinterpret_cast<hgb_image *>(d));
-    check(st, "SobelMagnitude::execute");
+    check(hgb_sobel_mag(&iv, &ov, mx_.coefficients(), my_.coefficients(), mx_.size_x(), (int)in_.mode(),
+                        (int)in_.constant(), sum, mx, current_stream()),
+          "SobelMagnitude::execute");
+    fetched_ = false;
   }
-  uchar reduce_output() override { return (uchar)host_[1]; }
+  // read the two scalars back (synchronises the current stream)
+  void fetch() {
+    execute();
+    if (fetched_) return;
+    unsigned long long tmp[2] = {0, 0};
+    check(hgb_image_read(scratch_.get(), tmp, current_stream()), "SobelMagnitude::reduced_data");
+    host_[0] = tmp[0];
+    host_[1] = tmp[1] & 0xffffffffull;
+    fetched_ = true;
+  }
+  uchar reduce_output() override {
+    fetch();
+    return (uchar)host_[1];
+  }
+  std::shared_ptr<hgb_image> scratch_;
+  bool fetched_ = false;
   Accessor<uchar> &in_;
   Mask<int> &mx_, &my_;
   unsigned long long host_[2] = {0, 0};
@@ -408,7 +478,7 @@ class ColorConversion : public Kernel<uchar> {
  protected:
   void launch() override {
     hgb_view iv = in_.image().view(), ov = this->out_view();
-    check(hgb_point_gray(&iv, &ov, wr_, wg_, wb_, sh_, nullptr), "ColorConversion::execute");
+    check(hgb_point_gray(&iv, &ov, wr_, wg_, wb_, sh_, current_stream()), "ColorConversion::execute");
   }
   Accessor<uchar4> &in_;
   int wr_, wg_, wb_, sh_;
@@ -425,10 +495,10 @@ class Copy : public Kernel<T> {
     hgb_view iv = in_.image().view(), ov = this->out_view();
     if (in_.interpolation() == Interpolate::NO) {
       check(hgb_image_copy_region(in_.image().handle(), &in_.window(), this->it_.image().handle(), this->out_window(),
-                                  nullptr),
+                                  current_stream()),
             "Copy::execute");
     } else {
-      check(hgb_resample(&iv, &ov, (int)in_.interpolation(), nullptr), "Copy::execute");
+      check(hgb_resample(&iv, &ov, (int)in_.interpolation(), current_stream()), "Copy::execute");
     }
   }
   Accessor<T> &in_;
@@ -446,10 +516,10 @@ class Difference : public Kernel<T> {
     if (b_.interpolation() != Interpolate::NO) {
       Image<T> tmp(ov.width, ov.height);
       hgb_view tv = tmp.view();
-      check(hgb_resample(&bv, &tv, (int)b_.interpolation(), nullptr), "Difference::execute");
-      check(hgb_point_binary(0, &av, &tv, &ov, 1.0f, 1.0f, nullptr), "Difference::execute");
+      check(hgb_resample(&bv, &tv, (int)b_.interpolation(), current_stream()), "Difference::execute");
+      check(hgb_point_binary(0, &av, &tv, &ov, 1.0f, 1.0f, current_stream()), "Difference::execute");
     } else {
-      check(hgb_point_binary(0, &av, &bv, &ov, 1.0f, 1.0f, nullptr), "Difference::execute");
+      check(hgb_point_binary(0, &av, &bv, &ov, 1.0f, 1.0f, current_stream()), "Difference::execute");
     }
   }
   Accessor<T> &a_, &b_;
@@ -569,8 +639,8 @@ class LaplacianPyramidBatch {
     check(hgb_pyramid_level_view(plan_.get(), image, level, &g, &l), "pyramid view");
     return l;
   }
-  void decompose(int mode = 0) { check(hgb_pyramid_decompose(plan_.get(), mode, nullptr), "pyramid decompose"); }
-  void collapse() { check(hgb_pyramid_collapse(plan_.get(), nullptr), "pyramid collapse"); }
+  void decompose(int mode = 0) { check(hgb_pyramid_decompose(plan_.get(), mode, current_stream()), "pyramid decompose"); }
+  void collapse() { check(hgb_pyramid_collapse(plan_.get(), current_stream()), "pyramid collapse"); }
 
  private:
   std::shared_ptr<hgb_pyramid_plan> plan_;

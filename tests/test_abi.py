@@ -82,7 +82,7 @@ def test_samples_compile_and_link(hgb_lib, tmp_path):
     import subprocess
 
     lib = os.path.join(ROOT, "hipacc_gb300")
-    for name in ("gaussian_blur", "sobel", "color_reduce", "pyramid", "bilateral"):
+    for name in ("gaussian_blur", "sobel", "color_reduce", "pyramid", "bilateral", "graph"):
         r = subprocess.run(["g++", "-O1", "-std=c++17", "-I", os.path.join(ROOT, "include"),
                             os.path.join(ROOT, "tests", "samples", name + ".cpp"), "-L", lib, "-lhipacc_gb300",
                             "-Wl,-rpath," + lib, "-o", str(tmp_path / name)], capture_output=True, text=True)

@@ -9,7 +9,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-SAMPLES = ["gaussian_blur", "sobel", "color_reduce", "pyramid", "bilateral"]
+SAMPLES = ["gaussian_blur", "sobel", "color_reduce", "pyramid", "bilateral", "graph"]
 
 
 @pytest.fixture(scope="module")
