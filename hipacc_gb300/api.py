@@ -136,9 +136,12 @@ def convert(inp, dtype, stream=None):
     return out
 
 
+INTERPOLATE = {"nn": 1, "lf": 2, "b5": 3, "cf": 4, "l3": 5}  # hipacc::Interpolate numbering
+
+
 def resample(inp, out, mode="lf", stream=None):
     vi, vo = view(inp), view(out)
-    L.call("hgb_resample", C.byref(vi), C.byref(vo), 1 if mode == "nn" else 2, _stream(stream))
+    L.call("hgb_resample", C.byref(vi), C.byref(vo), INTERPOLATE[mode], _stream(stream))
     return out
 
 

@@ -215,6 +215,75 @@ __device__ __forceinline__ float lf_sample(const float *src, int64_t sp, int sw,
   return r;
 }
 
+// B5 / CF / L3 accessors of the CPU back end (runtime/hipacc_cpu_interpolate.hpp:
+// binomial5, bicubic_spline with a = -0.5, lanczos with l = 3), every product
+// and sum rounded separately in the macros' order, taps clamped to the image.
+// B5: xb = x_mapped, columns x_int-1..x_int+2, weight b5((x_frac + 1) - j);
+// CF: xb = x_mapped - 0.5, columns x_int-1..x_int+2, weight cubic((x_frac - 1) + j);
+// L3: xb = x_mapped - 0.5, columns x_int-2..x_int+3 and rows y_int-1..y_int+4,
+//     weight lanczos((frac - 2) + j); the reference gives the fifth tap of the
+//     second row the sixth tap's weight, and so does this kernel.
+__device__ __forceinline__ float wt_b5(float d) {
+  d = fabsf(d);
+  return d < 0.5f ? 0.75f : (d < 1.0f ? 0.5f : (d < 1.5f ? 0.125f : 0.0f));
+}
+__device__ __forceinline__ float wt_cf(float d) {
+  d = fabsf(d);
+  const float a = -0.5f;
+  if (d < 1.0f) {
+    const float t1 = __fmul_rn(__fmul_rn(__fmul_rn(a + 2.0f, d), d), d);
+    const float t2 = __fmul_rn(__fmul_rn(a + 3.0f, d), d);
+    return __fadd_rn(__fsub_rn(t1, t2), 1.0f);
+  }
+  if (d < 2.0f) {
+    const float t1 = __fmul_rn(__fmul_rn(__fmul_rn(a, d), d), d);
+    const float t2 = __fmul_rn(__fmul_rn(5.0f * a, d), d);
+    const float t3 = __fmul_rn(8.0f * a, d);
+    return __fsub_rn(__fadd_rn(__fsub_rn(t1, t2), t3), 4.0f * a);
+  }
+  return 0.0f;
+}
+__device__ __forceinline__ float wt_l3(float d) {
+  d = fabsf(d);
+  if (d == 0.0f) return 1.0f;
+  if (d < 3.0f) {
+    // the reference's pi is the double of <cmath>: arguments and denominator in double
+    const double pi = 3.14159265358979323846, ad = (double)d;
+    const float s1 = sinf((float)(pi * ad / 3.0)), s2 = sinf((float)(pi * ad));
+    return (float)((double)__fmul_rn(3.0f, __fmul_rn(s1, s2)) / (pi * pi * ad * ad));
+  }
+  return 0.0f;
+}
+
+__device__ float filtered_sample(const float *src, int64_t sp, int sw, int sh, float xm, float ym, int imode) {
+  const bool b5 = imode == 3, l3 = imode == 5;
+  float xb = b5 ? xm : xm - 0.5f, yb = b5 ? ym : ym - 0.5f;
+  xb = xb < 0.0f ? 0.0f : xb;
+  yb = yb < 0.0f ? 0.0f : yb;
+  const int xi = (int)xb, yi = (int)yb;
+  const float xf = xb - (float)xi, yf = yb - (float)yi;
+  const int n = l3 ? 6 : 4;
+  const int cx0 = l3 ? xi - 2 : xi - 1, cy0 = yi - 1;
+  const float tx = b5 ? xf + 1.0f : (l3 ? xf - 2.0f : xf - 1.0f);
+  const float ty = b5 ? yf + 1.0f : (l3 ? yf - 2.0f : yf - 1.0f);
+  auto w = [&](float d) { return b5 ? wt_b5(d) : (l3 ? wt_l3(d) : wt_cf(d)); };
+  float out = 0.0f;
+  for (int k = 0; k < n; ++k) {
+    const int y = min(max(cy0 + k, 0), sh - 1);
+    const float *row = reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + y * sp);
+    float acc = 0.0f;
+    for (int j = 0; j < n; ++j) {
+      const int x = min(max(cx0 + j, 0), sw - 1);
+      const int jw = (l3 && k == 1 && j == 4) ? 5 : j;
+      const float p = __fmul_rn(__ldg(row + x), w(b5 ? __fsub_rn(tx, (float)jw) : __fadd_rn(tx, (float)jw)));
+      acc = j == 0 ? p : __fadd_rn(acc, p);
+    }
+    const float q = __fmul_rn(acc, w(b5 ? __fsub_rn(ty, (float)k) : __fadd_rn(ty, (float)k)));
+    out = k == 0 ? q : __fadd_rn(out, q);
+  }
+  return out;
+}
+
 __global__ void __launch_bounds__(256) resample_kernel(const char *in, int64_t ip, int64_t ibs, int sw, int sh,
                                                        char *out, int64_t op, int64_t obs, int dw, int dh, int batch,
                                                        int imode) {
@@ -232,8 +301,10 @@ __global__ void __launch_bounds__(256) resample_kernel(const char *in, int64_t i
       xx = min(max(xx, 0), sw - 1);
       yy = min(max(yy, 0), sh - 1);
       v = __ldg(reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + yy * ip) + xx);
-    } else {
+    } else if (imode == 2) {
       v = lf_sample(src, ip, sw, sh, mapped(sx, x), mapped(sy, y));
+    } else {
+      v = filtered_sample(src, ip, sw, sh, mapped(sx, x), mapped(sy, y), imode);
     }
     reinterpret_cast<float *>(out + b * obs + y * op)[x] = v;
   }
@@ -427,7 +498,7 @@ extern "C" int hgb_resample(const hgb_view *in, const hgb_view *out, int imode, 
   rc = check_view(out, "out");
   if (rc) return rc;
   HGB_REQUIRE(in->dtype == HGB_F32 && out->dtype == HGB_F32, "hgb_resample: f32 expected");
-  HGB_REQUIRE(imode == 1 || imode == 2, "hgb_resample: imode must be 1 (NN) or 2 (LF)");
+  HGB_REQUIRE(imode >= 1 && imode <= 5, "hgb_resample: imode must be 1 (NN), 2 (LF), 3 (B5), 4 (CF) or 5 (L3)");
   HGB_REQUIRE(in->batch == out->batch, "hgb_resample: batch mismatch");
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t n = (int64_t)out->width * out->height * out->batch;

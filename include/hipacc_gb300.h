@@ -229,9 +229,12 @@ HGB_API int hgb_point_binary(int op, const hgb_view *a, const hgb_view *b, const
 /* Storage conversion between f32, bf16, f16 (round to nearest even) and u8. */
 HGB_API int hgb_convert(const hgb_view *in, const hgb_view *out, void *stream);
 
-/* Resampling accessor read as a point operator (Interpolate::NN / LF,
- * lib/AST/Interpolate.cpp:85-113, runtime/hipacc_cu_interpolate.hpp:173-216):
- * out(x,y) = in at the mapped position, CLAMP taps.  imode 1 = NN, 2 = LF. */
+/* Resampling accessor read as a point operator (Interpolate::NN / LF / B5 /
+ * CF / L3, lib/AST/Interpolate.cpp:85-113, runtime/hipacc_cu_interpolate.hpp:173-616,
+ * runtime/hipacc_cpu_interpolate.hpp:157-520): out(x,y) = in at the mapped
+ * position scale/2 + scale*x, CLAMP taps.  imode 1 = NN, 2 = LF (bilinear),
+ * 3 = B5 (binomial, 4x4 taps), 4 = CF (cubic a = -0.5, 4x4), 5 = L3 (Lanczos-3,
+ * 6x6, the reference's tap weights).  f32 images. */
 HGB_API int hgb_resample(const hgb_view *in, const hgb_view *out, int imode, void *stream);
 
 /* ------------------------------------------------------------------ */

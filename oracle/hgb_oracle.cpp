@@ -463,6 +463,89 @@ void orc_bilateral_f64(const double *in, int w, int h, long stride, double *out,
   bilateral<double>(in, w, h, stride, out, out_stride, smask, size, sigma_r, bmode, cval, 0, nthreads);
 }
 
+// ------------------------------------------------------------------ B5 / CF / L3
+// The CPU back end's binomial, cubic and Lanczos-3 filtering accessors
+// (runtime/hipacc_cpu_interpolate.hpp:199-520: binomial5, bicubic_spline with
+// a = -0.5, lanczos with l = 3 and the <cmath> M_PI) with clamped taps over
+// the whole image.  Every product and sum is rounded separately, left to
+// right, as the macros' expressions; taps and weights per mode:
+//   B5: xb = x_mapped,       columns x_int-1..x_int+2, weight b5((x_frac + 1) - j)
+//   CF: xb = x_mapped - 0.5, columns x_int-1..x_int+2, weight cubic((x_frac - 1) + j)
+//   L3: xb = x_mapped - 0.5, columns x_int-2..x_int+3, weight lanczos((x_frac - 2) + j),
+//       rows y_int-1..y_int+4 with weight lanczos((y_frac - 2) + k) (the macro's row offset);
+//       the fifth tap of the second row carries the sixth tap's weight
+//       lanczos((x_frac - 2) + 5), as in the macro (and the DSL's accessor)
+static float wt_binomial5(float d) {
+  d = std::fabs(d);
+  if (d < 0.5f) return 6.0f / 8.0f;
+  if (d < 1.0f) return 4.0f / 8.0f;
+  if (d < 1.5f) return 1.0f / 8.0f;
+  return 0.0f;
+}
+
+static float wt_cubic(float d) {
+  d = std::fabs(d);
+  const float a = -0.5f;
+  if (d < 1.0f) return (a + 2.0f) * d * d * d - (a + 3.0f) * d * d + 1.0f;
+  if (d < 2.0f) return a * d * d * d - 5.0f * a * d * d + 8.0f * a * d - 4.0f * a;
+  return 0.0f;
+}
+
+static float wt_lanczos(float d) {
+  d = std::fabs(d);
+  const float l = 3.0f;
+  if (d == 0.0f) return 1.0f;
+  if (d < l) {
+    // M_PI is the double of <cmath>: the arguments and the denominator are
+    // evaluated in double, the sines in float
+    const float s1 = std::sin((float)(M_PI * (double)d / (double)l));
+    const float s2 = std::sin((float)(M_PI * (double)d));
+    return (float)((double)(l * (s1 * s2)) / (M_PI * M_PI * (double)d * (double)d));
+  }
+  return 0.0f;
+}
+
+static inline float clamp_tap(const float *src, int sw, int sh, int x, int y) {
+  x = x < 0 ? 0 : (x >= sw ? sw - 1 : x);
+  y = y < 0 ? 0 : (y >= sh ? sh - 1 : y);
+  return src[(long)y * sw + x];
+}
+
+static float interp_filtered(const float *src, int sw, int sh, float xm, float ym, int mode) {
+  const bool b5 = mode == 3, l3 = mode == 5;
+  float xb = b5 ? xm : xm - 0.5f, yb = b5 ? ym : ym - 0.5f;
+  if (xb < 0.0f) xb = 0.0f;
+  if (yb < 0.0f) yb = 0.0f;
+  const int xi = (int)xb, yi = (int)yb;
+  const float xf = xb - (float)xi, yf = yb - (float)yi;
+  const int n = l3 ? 6 : 4;                        // taps per row / rows
+  const int cx0 = l3 ? xi - 2 : xi - 1, cy0 = yi - 1;  // first column / row
+  auto w = [&](float d) { return b5 ? wt_binomial5(d) : (l3 ? wt_lanczos(d) : wt_cubic(d)); };
+  const float tx = b5 ? xf + 1.0f : (l3 ? xf - 2.0f : xf - 1.0f);
+  const float ty = b5 ? yf + 1.0f : (l3 ? yf - 2.0f : yf - 1.0f);
+  float out = 0.0f;
+  for (int k = 0; k < n; ++k) {
+    float row = 0.0f;
+    for (int j = 0; j < n; ++j) {
+      const int jw = (l3 && k == 1 && j == 4) ? 5 : j;  // the macro's weight for this tap
+      const float p = clamp_tap(src, sw, sh, cx0 + j, cy0 + k) * w(b5 ? tx - (float)jw : tx + (float)jw);
+      row = j == 0 ? p : row + p;
+    }
+    const float q = row * w(b5 ? ty - (float)k : ty + (float)k);
+    out = k == 0 ? q : out + q;
+  }
+  return out;
+}
+
+void orc_resample_filtered_f32(const float *src, int sw, int sh, float *dst, int dw, int dh, int mode, int contract) {
+  const float sx = (float)sw / (float)dw, sy = (float)sh / (float)dh;
+  for (int y = 0; y < dh; ++y) {
+    const float ym = mapped_coord(sy, y, contract);
+    for (int x = 0; x < dw; ++x)
+      dst[(long)y * dw + x] = interp_filtered(src, sw, sh, mapped_coord(sx, x, contract), ym, mode);
+  }
+}
+
 void orc_resample_nn_f32(const float *src, int sw, int sh, float *dst, int dw, int dh, int contract) {
   resample_nn<float>(src, sw, sh, dst, dw, dh, contract);
 }

@@ -99,6 +99,10 @@ void orc_bilateral_f64(const double *in, int w, int h, long stride, double *out,
  * (lib/AST/Interpolate.cpp:85-113, runtime/hipacc_cpu_interpolate.hpp:157-197). */
 void orc_resample_nn_f32(const float *src, int sw, int sh, float *dst, int dw, int dh, int contract);
 void orc_resample_lf_f32(const float *src, int sw, int sh, float *dst, int dw, int dh, int contract);
+/* B5 / CF / L3 resampling accessors (mode 3 / 4 / 5, hipacc::Interpolate
+ * numbering) of the CPU back end with clamped taps; `contract` applies to the
+ * mapped coordinate only (the GPU maps with one fused multiply-add). */
+void orc_resample_filtered_f32(const float *src, int sw, int sh, float *dst, int dw, int dh, int mode, int contract);
 
 /* Laplacian pyramid (samples-public/5_Other/Gaussian_Laplacian_Pyramid/src/main.cpp:199-248).
  * gauss[l] (l = 0..levels-1) and lap[l] (l = 0..levels-2) are caller buffers of

@@ -78,6 +78,7 @@ def lib():
                                         C.c_double, C.c_int, C.c_double, C.c_int]
         L.orc_resample_nn_f32.argtypes = [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, C.c_int]
         L.orc_resample_lf_f32.argtypes = [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, C.c_int]
+        L.orc_resample_filtered_f32.argtypes = [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_pyramid_decompose_f32.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int,
                                                 C.c_int, f32p, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_pyramid_decompose_f64.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int,
@@ -117,6 +118,7 @@ def ref():
             getattr(R, n).argtypes = [f32p, C.c_int, C.c_int]
             getattr(R, n).restype = C.c_float
         R.ref_cpu_red_cores_omp.restype = C.c_int
+        R.ref_cpu_interp_f32.argtypes = [C.c_int, f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int]
         for n in ("ref_cpu_histogram_f32_serial", "ref_cpu_histogram_f32_omp"):
             getattr(R, n).argtypes = [f32p, C.c_int, C.c_int, C.c_uint, u32p]
         _ref = R
@@ -243,6 +245,17 @@ def bilateral(img, smask, sigma_r, boundary=CLAMP, const=0.0, contract=1, nthrea
         lib().orc_bilateral_f64(img, w, h, w, out, w, np.ascontiguousarray(smask, np.float64), size, sigma_r,
                                 boundary, const, nt)
     return out
+
+
+FILTERED = {"b5": 3, "cf": 4, "l3": 5}
+
+
+def resample_filtered(src, dw, dh, mode, contract=1):
+    """B5 / CF / L3 resampling accessors of the CPU back end (clamped taps)."""
+    src = np.ascontiguousarray(src, np.float32)
+    dst = np.zeros((dh, dw), np.float32)
+    lib().orc_resample_filtered_f32(src, src.shape[1], src.shape[0], dst, dw, dh, FILTERED[mode], contract)
+    return dst
 
 
 def resample(src, dw, dh, mode="lf", contract=1):

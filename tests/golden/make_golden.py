@@ -109,6 +109,14 @@ def main():
         bins = np.zeros(nb, np.uint32)
         R.ref_cpu_histogram_f32_serial(hist, 41, 29, nb, bins)
         out[f"hist_{nb}"] = bins
+    # B5 / CF / L3 resampling accessors through the CPU back end's own macros
+    for (sh, sw, dh, dw) in ((17, 23, 40, 31), (30, 50, 11, 19)):
+        src = rng.random((sh, sw), dtype=np.float32)
+        out[f"interp_{sw}x{sh}_{dw}x{dh}_in"] = src
+        for name, m in (("b5", 3), ("cf", 4), ("l3", 5)):
+            dst = np.zeros((dh, dw), np.float32)
+            assert R.ref_cpu_interp_f32(m, src, sw, sh, dst, dw, dh) == 0
+            out[f"interp_{name}_{sw}x{sh}_{dw}x{dh}"] = dst
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path), "bytes,", len(out), "arrays")
 

@@ -55,6 +55,17 @@ def test_histogram_golden(oracle, golden):
     assert np.array_equal(oracle.histogram(u8, 256), oracle.histogram(u8.astype(np.float32), 256))
 
 
+def test_filtered_resampling_golden(oracle, golden):
+    """B5 / CF / L3 accessors: the restatement against the CPU back end's own
+    macros (including the Lanczos weight the reference gives the fifth tap of
+    the second row)."""
+    for (sh, sw, dh, dw) in ((17, 23, 40, 31), (30, 50, 11, 19)):
+        src = golden[f"interp_{sw}x{sh}_{dw}x{dh}_in"]
+        for mode in ("b5", "cf", "l3"):
+            got = oracle.resample_filtered(src, dw, dh, mode, contract=0)
+            assert np.array_equal(got, golden[f"interp_{mode}_{sw}x{sh}_{dw}x{dh}"]), mode
+
+
 def test_bilateral_golden(oracle, golden):
     O = oracle
     for size in (5, 13):

@@ -1,0 +1,43 @@
+"""GPU parity of the resampling accessors B5 / CF / L3 (Interpolate::B5, CF,
+L3 read as a point operator) against the oracle's restatement of the CPU back
+end's macros, which the golden vectors pin to the reference itself.
+
+B5 and CF are bit-exact (every product and sum rounded as in the macros; the
+mapped coordinate is one fused multiply-add on both sides, contract=1).  L3
+evaluates sinf, whose CUDA and libm results differ by an ulp or two, so it is
+held to L3_TOL absolute on [0, 1] data."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+L3_TOL = 2e-6
+
+
+@pytest.mark.parametrize("shape", [((17, 23), (40, 31)), ((64, 48), (16, 20)), ((300, 500), (611, 997)),
+                                   ((9, 9), (9, 9)), ((5, 7), (3, 2))])
+@pytest.mark.parametrize("mode", ["b5", "cf", "l3"])
+def test_filtered_resampling(gpu, oracle, shape, mode):
+    (sh, sw), (dh, dw) = shape
+    rng = np.random.default_rng(sh * 1000 + dw)
+    src = rng.random((sh, sw), dtype=np.float32)
+    out = torch.empty((dh, dw), dtype=torch.float32, device="cuda")
+    gpu.resample(torch.from_numpy(src).cuda(), out, mode=mode)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    ref = oracle.resample_filtered(src, dw, dh, mode, contract=1)
+    if mode == "l3":
+        assert np.max(np.abs(got - ref)) <= L3_TOL
+    else:
+        assert np.array_equal(got, ref)
+
+
+def test_filtered_resampling_batch(gpu, oracle):
+    rng = np.random.default_rng(77)
+    src = rng.random((3, 40, 60), dtype=np.float32)
+    out = torch.empty((3, 25, 90), dtype=torch.float32, device="cuda")
+    gpu.resample(torch.from_numpy(src).cuda(), out, mode="cf")
+    torch.cuda.synchronize()
+    for b in range(3):
+        assert np.array_equal(out[b].cpu().numpy(), oracle.resample_filtered(src[b], 90, 25, "cf", contract=1))
