@@ -12,7 +12,9 @@
 // Level sizes are floor(w / 2^l) (dsl/pyramid.hpp:103-114).
 //
 // GB300 form: one level-tile kernel does all three for a 64 x 32 tile of L_l:
-// it stages the G_l region it needs once in shared memory, evaluates the blur
+// it stages the G_l region it needs once in shared memory with one TMA load
+// (a tensor map per image and level, built with the plan; cells outside the
+// level are patched through the boundary remap), evaluates the blur
 // only at the nearest-neighbour sample positions of the G_{l+1} tile plus a
 // one-pixel halo (kept in shared memory), writes the G_{l+1} pixels the tile
 // owns, and writes L_l from the staged G_l and the shared G_{l+1} values.
@@ -44,6 +46,9 @@ namespace {
 constexpr int PY_TW = 64, PY_TH = 32;              // L_l tile
 constexpr int PY_GW = PY_TW / 2 + 2, PY_GH = PY_TH / 2 + 2;  // G_{l+1} tile + halo
 constexpr int PY_SW = PY_TW + 12, PY_SH = PY_TH + 12;        // staged G_l region bound
+// TMA box of the staged region: its x origin is rounded down to a multiple of
+// 4 floats (16 bytes), so the box is 4 floats wider than the region bound
+constexpr int PY_BW = PY_SW + 4, PY_BH = PY_SH;
 constexpr int PY_THREADS = 256;
 
 struct LevelMeta {
@@ -60,6 +65,7 @@ struct PyrTile {
 
 struct PyrParams {
   const LevelMeta *meta;  // [img * levels + l]
+  const CUtensorMap *maps;  // [img * levels + l]: G_l tensor maps, box PY_BW x PY_BH
   const PyrTile *tiles;
   int ntiles;
   int levels;
@@ -107,8 +113,9 @@ __device__ __forceinline__ LfTap lf_tap(float s, int x, int n, int origin) {
 }
 
 // One 64 x 32 tile of L_level (and the owned part of G_{level+1}).
-__device__ void pyr_tile(const PyrParams &p, const PyrTile t, float *stage, float *gt, LfTap *cols, LfTap *rows,
-                         bool coherent) {
+// `bar` is the CTA's mbarrier and `phase` its next phase parity.
+__device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, float *gt, LfTap *cols, LfTap *rows,
+                         uint64_t *bar, unsigned &phase, bool coherent) {
   const LevelMeta A = p.meta[t.img * p.levels + t.level];
   const LevelMeta B = p.meta[t.img * p.levels + t.level + 1];
   const int wl = A.w, hl = A.h, wn = B.w, hn = B.h;
@@ -121,49 +128,81 @@ __device__ void pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
     int v = (int)__fmaf_rn(S, (float)x, S * 0.5f);
     return v < lim ? v : lim - 1;
   };
-  const int rx0 = nn(Sx, gx0, wl) - 2, rx1 = nn(Sx, gx1 - 1, wl) + 3;
-  const int ry0 = nn(Sy, gy0, hl) - 2, ry1 = nn(Sy, gy1 - 1, hl) + 3;
-  const int sw = rx1 - rx0, sh = ry1 - ry0;  // <= PY_SW, PY_SH
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // ---- stage G_l[ry0..ry1) x [rx0..rx1): a warp per row, lanes along it;
-  // only tiles whose region leaves the level go through the boundary remap
-  const bool inside = rx0 >= 0 && rx1 <= wl && ry0 >= 0 && ry1 <= hl;
-  for (int r = warp; r < sh; r += PY_THREADS / 32) {
-    const int y = ry0 + r;
-    float *dst = stage + r * PY_SW;
-    if (inside) {
-      const float *src = A.g + (int64_t)y * A.pitch + rx0;
-      for (int q = lane; q < sw; q += 32) dst[q] = ld_level(src + q, coherent);
-    } else {
-      const int yy = remap(p.bmode, y, 0, hl);
-      for (int q = lane; q < sw; q += 32) {
-        const int xx = remap(p.bmode, rx0 + q, 0, wl);
-        dst[q] = (yy == (int)0x80000000 || xx == (int)0x80000000) ? 0.0f
-                                                                  : ld_level(A.g + (int64_t)yy * A.pitch + xx, coherent);
-      }
-    }
+  const int rx0 = nn(Sx, gx0, wl) - 2;
+  const int ry0 = nn(Sy, gy0, hl) - 2;
+  // ---- stage the G_l box [ry0, ry0 + BH) x [bx0, bx0 + BW) with one TMA load
+  const int bx0 = rx0 & ~3, ox = rx0 - bx0;
+  if (threadIdx.x == 0) {
+    // in the persistent form G_l was written by other CTAs of this launch
+    // (generic stores, acquired by the level wait): order them before the
+    // tensor copy's read
+    if (coherent) asm volatile("fence.proxy.async.global;" ::: "memory");
+    mbar_expect_tx(bar, PY_BW * PY_BH * 4);
+    tma_load_3d(stage, &p.maps[t.img * p.levels + t.level], bx0, ry0, 0, bar);
   }
-  // linear-filtering taps of the tile's columns and rows
+  // linear-filtering taps of the tile's columns and rows (while the box lands)
   if (threadIdx.x < PY_TW)
     cols[threadIdx.x] = lf_tap(sx, t.x0 + threadIdx.x, wn, gx0);
   else if (threadIdx.x < PY_TW + PY_TH)
     rows[threadIdx.x - PY_TW] = lf_tap(sy, t.y0 + threadIdx.x - PY_TW, hn, gy0);
-  __syncthreads();
+  const bool landed = mbar_wait(bar, phase);
+  phase ^= 1u;
+  if (__syncthreads_or(!landed)) {
+    if (threadIdx.x == 0) {
+      record_status(p.status, HGB_ERR_TIMEOUT);
+      mbar_wait(bar, phase ^ 1u);  // the copy may still land: wait once more (bounded)
+    }
+    return false;
+  }
+  if (bx0 < 0 || bx0 + PY_BW > wl || ry0 < 0 || ry0 + PY_BH > hl) {
+    // box cells outside the level (zero-filled by TMA) through the boundary
+    // remap: left / right columns, top / bottom rows
+    const int nl = max(0, min(PY_BW, -bx0)), rs = max(0, min(PY_BW, wl - bx0));
+    const int nt = max(0, min(PY_BH, -ry0)), bs = max(0, min(PY_BH, hl - ry0));
+    const int ncl = nl * PY_BH, ncr = (PY_BW - rs) * PY_BH, nrt = nt * PY_BW, nrb = (PY_BH - bs) * PY_BW;
+    for (int c = threadIdx.x; c < ncl + ncr + nrt + nrb; c += PY_THREADS) {
+      int r, q;
+      if (c < ncl) {
+        r = c / nl;
+        q = c - r * nl;
+      } else if (c < ncl + ncr) {
+        const int d = c - ncl, n = PY_BW - rs;
+        r = d / n;
+        q = rs + (d - r * n);
+      } else if (c < ncl + ncr + nrt) {
+        const int d = c - ncl - ncr;
+        r = d / PY_BW;
+        q = d - r * PY_BW;
+      } else {
+        const int d = c - ncl - ncr - nrt;
+        const int rr = d / PY_BW;
+        r = bs + rr;
+        q = d - rr * PY_BW;
+      }
+      const int yy = remap(p.bmode, ry0 + r, 0, hl), xx = remap(p.bmode, bx0 + q, 0, wl);
+      stage[r * PY_BW + q] = (yy == (int)0x80000000 || xx == (int)0x80000000)
+                                 ? 0.0f
+                                 : ld_level(A.g + (int64_t)yy * A.pitch + xx, coherent);
+    }
+    __syncthreads();
+  }
   // ---- G_{l+1} on the tile + halo: blur at the nearest-neighbour positions
   const int gw = gx1 - gx0, gh = gy1 - gy0;
-  for (int c = threadIdx.x; c < gw * gh; c += PY_THREADS) {
-    const int r = c / gw, q = c - r * gw;
+  for (int c = threadIdx.x; c < PY_GW * PY_GH; c += PY_THREADS) {
+    const int r = c / PY_GW, q = c - r * PY_GW;  // constant divisor
+    if (q >= gw || r >= gh) continue;
     const int xp = gx0 + q, yp = gy0 + r;
-    const int cx = nn(Sx, xp, wl) - 2 - rx0, cy = nn(Sy, yp, hl) - 2 - ry0;
+    const int cx = nn(Sx, xp, wl) - 2 - rx0 + ox, cy = nn(Sy, yp, hl) - 2 - ry0;
+    const float *src = stage + cy * PY_BW + cx;
     float acc = 0.0f;
 #pragma unroll
     for (int my = 0; my < 5; ++my)
 #pragma unroll
-      for (int mx = 0; mx < 5; ++mx) acc = __fmaf_rn(p.mask[my * 5 + mx], stage[(cy + my) * PY_SW + cx + mx], acc);
+      for (int mx = 0; mx < 5; ++mx) acc = __fmaf_rn(p.mask[my * 5 + mx], src[my * PY_BW + mx], acc);
     gt[r * PY_GW + q] = acc;
     // owned pixels of G_{l+1}: x' in [x0/2, x0/2 + TW/2), y' likewise
     if (xp >= t.x0 / 2 && xp < t.x0 / 2 + PY_TW / 2 && yp >= t.y0 / 2 && yp < t.y0 / 2 + PY_TH / 2)
-      B.g[(int64_t)yp * B.pitch + xp] = acc;
+      __stwb(B.g + (int64_t)yp * B.pitch + xp, acc);
   }
   __syncthreads();
   // ---- L_l = G_l - LF(G_{l+1}): a thread per column, rows strided
@@ -171,6 +210,7 @@ __device__ void pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
   const int x = t.x0 + tx;
   if (x < wl) {
     const LfTap cx = cols[tx];
+    const float *gcol = stage + (x - rx0 + ox);
     for (int r = threadIdx.x / PY_TW; r < PY_TH; r += PY_THREADS / PY_TW) {
       const int y = t.y0 + r;
       if (y >= hl) break;
@@ -181,25 +221,39 @@ __device__ void pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
       lf = __fmaf_rn(wb, gt[cy.a * PY_GW + cx.c], lf);
       lf = __fmaf_rn(wc, gt[cy.c * PY_GW + cx.a], lf);
       lf = __fmaf_rn(wd, gt[cy.c * PY_GW + cx.c], lf);
-      const float g = stage[(y - ry0) * PY_SW + (x - rx0)];
-      A.lap[(int64_t)y * A.pitch + x] = __fsub_rn(g, lf);
+      __stwb(A.lap + (int64_t)y * A.pitch + x, __fsub_rn(gcol[(y - ry0) * PY_BW], lf));
     }
   }
+  return true;
 }
 
 __global__ void __launch_bounds__(PY_THREADS) pyr_level_kernel(const __grid_constant__ PyrParams p, int first) {
-  __shared__ float stage[PY_SW * PY_SH];
+  __shared__ __align__(128) float stage[PY_BW * PY_BH];
   __shared__ float gt[PY_GW * PY_GH];
   __shared__ LfTap cols[PY_TW], rows[PY_TH];
-  pyr_tile(p, p.tiles[first + blockIdx.x], stage, gt, cols, rows, false);
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  unsigned phase = 0;
+  pyr_tile(p, p.tiles[first + blockIdx.x], stage, gt, cols, rows, &bar, phase, false);
 }
 
 __global__ void __launch_bounds__(PY_THREADS) pyr_persistent_kernel(const __grid_constant__ PyrParams p) {
-  __shared__ float stage[PY_SW * PY_SH];
+  __shared__ __align__(128) float stage[PY_BW * PY_BH];
   __shared__ float gt[PY_GW * PY_GH];
   __shared__ LfTap cols[PY_TW], rows[PY_TH];
+  __shared__ __align__(8) uint64_t bar;
   __shared__ int s_t;
   __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  unsigned phase = 0;
   for (;;) {
     if (threadIdx.x == 0) {
       const int t = (int)atomicAdd(p.work, 1u);
@@ -227,7 +281,7 @@ __global__ void __launch_bounds__(PY_THREADS) pyr_persistent_kernel(const __grid
     const int t = s_t;
     if (t >= p.ntiles) return;
     const PyrTile tl = p.tiles[t];
-    if (s_ok) pyr_tile(p, tl, stage, gt, cols, rows, true);
+    if (s_ok && !pyr_tile(p, tl, stage, gt, cols, rows, &bar, phase, true)) return;
     __syncthreads();
     if (threadIdx.x == 0) red_release_add(&p.done[tl.img * p.levels + tl.level], 1u);
   }
@@ -295,6 +349,7 @@ struct hgb_pyramid_plan {
   void *arena = nullptr;           // all levels of all images
   void *tmp = nullptr;             // blur buffer of the reference launch structure
   LevelMeta *d_meta = nullptr;
+  CUtensorMap *d_maps = nullptr;   // G_l tensor maps, [img * levels + l]
   PyrTile *d_tiles = nullptr;
   int *d_ntiles = nullptr;
   unsigned int *d_ctrl = nullptr;  // done counters [n*levels] + claim counter
@@ -368,7 +423,24 @@ int hgb_pyramid_plan_create(int n_images, const int *widths, const int *heights,
     P->meta[k].g = (float *)((char *)P->arena + goff[k]);
     P->meta[k].lap = ((int)(k % levels) + 1 < levels) ? (float *)((char *)P->arena + loff[k]) : nullptr;
   }
-  e = cudaMemcpy(P->d_meta, P->meta.data(), P->meta.size() * sizeof(LevelMeta), cudaMemcpyHostToDevice);
+  // tensor maps of every Gaussian level a tile stages (box PY_BW x PY_BH)
+  std::vector<CUtensorMap> maps(P->meta.size());
+  memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+  for (size_t k = 0; k < P->meta.size(); ++k) {
+    if ((int)(k % levels) + 1 >= levels) continue;
+    const LevelMeta &m = P->meta[k];
+    const int rc = make_tensor_map_3d(&maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, m.g, m.w, m.h, 1,
+                                      (int64_t)m.pitch * 4, (int64_t)m.pitch * 4 * m.h, PY_BW, PY_BH);
+    if (rc != HGB_OK) {
+      hgb_pyramid_plan_destroy(P);
+      return rc;
+    }
+  }
+  e = cudaMalloc((void **)&P->d_maps, maps.size() * sizeof(CUtensorMap));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(P->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(P->d_meta, P->meta.data(), P->meta.size() * sizeof(LevelMeta), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(P->d_tiles, tiles.data(), tiles.size() * sizeof(PyrTile), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(P->d_ntiles, nil.data(), nil.size() * sizeof(int), cudaMemcpyHostToDevice);
@@ -390,6 +462,7 @@ int hgb_pyramid_plan_destroy(hgb_pyramid_plan *P) {
   cudaFree(P->arena);
   cudaFree(P->tmp);
   cudaFree(P->d_meta);
+  cudaFree(P->d_maps);
   cudaFree(P->d_tiles);
   cudaFree(P->d_ntiles);
   cudaFree(P->d_ctrl);
@@ -422,6 +495,7 @@ int hgb_pyramid_level_view(const hgb_pyramid_plan *P, int image, int level, hgb_
 static void fill_params(const hgb_pyramid_plan *P, PyrParams *p) {
   memset(p, 0, sizeof(*p));
   p->meta = P->d_meta;
+  p->maps = P->d_maps;
   p->tiles = P->d_tiles;
   p->ntiles = P->ntiles;
   p->levels = P->levels;
