@@ -157,21 +157,11 @@ extern "C" int hgb_histogram(const hgb_view *in, const hgb_window *win, unsigned
   const size_t copies = p.layout == 2 ? 32 : (p.layout == 1 ? HB_T / 32 : 1);
   const size_t smem = ((size_t)num_bins * copies + (in->dtype == HGB_U8 ? 256 * 32 : 0)) * 4;
   HGB_CHECK_CUDA(cudaMemsetAsync(bins, 0, (size_t)num_bins * 4, st));
-  static bool attr = false;
-  if (!attr) {
-    HGB_CHECK_CUDA(cudaFuncSetAttribute(hist_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)((kMaxBins + 256 * 32) * 4)));
-    HGB_CHECK_CUDA(cudaFuncSetAttribute(hist_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)(kMaxBins * 4)));
-    attr = true;
-  }
+  const void *kern = in->dtype == HGB_U8 ? (const void *)hist_kernel<uint8_t> : (const void *)hist_kernel<float>;
+  rc = ensure_dynamic_smem(kern, smem);
+  if (rc) return rc;
   const int64_t items = ((int64_t)w.width * w.height * in->batch + 15) / 16;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, in->dtype == HGB_U8 ? (const void *)hist_kernel<uint8_t>
-                                                                                : (const void *)hist_kernel<float>,
-                                                    HB_T, smem) != cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
+  const int per_sm = resident_ctas(kern, HB_T, smem);
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)num_sms() * per_sm, (items + HB_T - 1) / HB_T));
   cudaEvent_t ev = before_launch(st);
   if (in->dtype == HGB_U8)

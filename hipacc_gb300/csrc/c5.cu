@@ -587,14 +587,9 @@ extern "C" int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, cons
   p.tiles_y = (int)grid.y;
   cudaStream_t st = (cudaStream_t)stream;
   // persistent grids: one wave of resident CTAs walking the tiles
-  static int occ[3] = {0, 0, 0};
-  if (!occ[0]) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], c5_forward_kernel, C5_T, 0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], c5_bilateral_adjoint_kernel, C5_T, 0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], c5_conv_adjoint_kernel, C5_T, 0) != cudaSuccess)
-      occ[0] = occ[1] = occ[2] = 1;
-    for (int i = 0; i < 3; ++i) occ[i] = std::max(occ[i], 1);
-  }
+  const int occ[3] = {resident_ctas((const void *)c5_forward_kernel, C5_T, 0),
+                      resident_ctas((const void *)c5_bilateral_adjoint_kernel, C5_T, 0),
+                      resident_ctas((const void *)c5_conv_adjoint_kernel, C5_T, 0)};
   auto wave = [&](int k, int ntiles) { return std::max(1, std::min(ntiles, num_sms() * occ[k])); };
   cudaEvent_t ev = before_launch(st);
   if (mode == 0) {

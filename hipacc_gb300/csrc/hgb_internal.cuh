@@ -51,6 +51,11 @@ constexpr int kSlotReduce = 2;  // acc[2]; ticket[1]
 int workspace_get(size_t bytes, Workspace *ws);  // grows on demand
 
 int num_sms();
+// Per-device, thread-safe kernel set-up: raise a kernel's dynamic shared
+// memory limit (once per device and size), and its resident CTAs per SM for a
+// launch shape (cached per device).
+int ensure_dynamic_smem(const void *kernel, size_t bytes);
+int resident_ctas(const void *kernel, int threads, size_t smem);
 
 // ---------------------------------------------------------------- dtypes
 inline int dtype_size(int dt) {

@@ -422,10 +422,7 @@ extern "C" int hgb_point_gray(const hgb_view *in, const hgb_view *out, int wr, i
     return after_launch("gray_bulk_kernel", st, ev);
   }
   // one resident wave: every CTA owns one contiguous range
-  static int per_sm = 0;
-  if (!per_sm && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gray_kernel, 256, 0) != cudaSuccess)
-    per_sm = 4;
-  int grid = num_sms() * (per_sm > 0 ? per_sm : 4);
+  int grid = num_sms() * resident_ctas((const void *)gray_kernel, 256, 0);
   const int64_t need = (p.rs.nitems + 511) / 512;
   if (need < grid) grid = (int)(need > 0 ? need : 1);
   cudaEvent_t ev = before_launch(st);

@@ -7,7 +7,9 @@
 // of per-call cudaMalloc/cudaFree (runtime/hipacc_cu.tpp:331-391).
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -105,6 +107,34 @@ int workspace_get(size_t bytes, Workspace *ws) {
   }
   *ws = st.ws;
   return HGB_OK;
+}
+
+int ensure_dynamic_smem(const void *kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> done;
+  int dev = 0;
+  HGB_CHECK_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &have = done[{dev, kernel}];
+  if (have >= bytes) return HGB_OK;
+  HGB_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  have = bytes;
+  return HGB_OK;
+}
+
+int resident_ctas(const void *kernel, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, const void *, int, size_t>, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_tuple(dev, kernel, threads, smem);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n < 1) n = 1;
+  cache[key] = n;
+  return n;
 }
 
 int num_sms() {

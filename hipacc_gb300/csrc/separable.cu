@@ -258,13 +258,9 @@ int launch_sep_k(const SepParams &p0, int batch, cudaStream_t st) {
     p.use_tma = 1;
     p.status = device_status_word();
   }
-  static bool attr = false;
-  if (!attr) {
-    HGB_CHECK_CUDA(cudaFuncSetAttribute(separable_kernel<T, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)std::max(S::smem_tma, S::smem_ldg)));
-    attr = true;
-  }
   const size_t smem = p.use_tma ? S::smem_tma : S::smem_ldg;
+  const int rc = ensure_dynamic_smem((const void *)separable_kernel<T, K>, smem);
+  if (rc) return rc;
   dim3 grid(cdiv(p.w, SP_TW), cdiv(p.h, SP_TH), batch);
   cudaEvent_t ev = before_launch(st);
   separable_kernel<T, K><<<grid, SP_BX * SP_BY, smem, st>>>(p);
