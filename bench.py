@@ -478,6 +478,14 @@ def _gaussian(dev, peak_gbs, s, res, q):
     res["gaussian5x5_f32_1024_clamp_b64"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
                                              "achieved_gbs": 8 * px / us / 1e3, "frac_hbm": 8 * px / us / 1e3 / peak_gbs}
     del ins, outs
+    # the Gaussian-blur sample's own storage: u8 in and out, (uchar)(sum + 0.5f)
+    ins = [torch.randint(0, 256, (64, 1024, 1024), dtype=torch.uint8, device=dev) for _ in range(nb)]
+    outs = [torch.empty_like(x) for x in ins]
+    us = graph_time_us(lambda i: api.local_op(ins[i % nb], outs[i % nb], mask=m5, boundary=api.CLAMP, stream=s), nb,
+                       s, 1 if q else 10)
+    res["gaussian5x5_u8_1024_clamp_b64"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                            "achieved_gbs": 2 * px / us / 1e3, "frac_hbm": 2 * px / us / 1e3 / peak_gbs}
+    del ins, outs
 
 
 def _precision(dev, peak_gbs, s, res, q):

@@ -110,6 +110,15 @@ __host__ __device__ __forceinline__ int remap(int mode, int idx, int lo, int hi)
 }
 
 template <typename T> struct Storage;
+// u8 pixels: widened exactly; written as the samples' (uchar)(x + 0.5f), with
+// values outside [0, 255] saturated (the C cast leaves them undefined)
+template <> struct Storage<uint8_t> {
+  static __device__ __forceinline__ float load(const uint8_t *p) { return (float)__ldg(p); }
+  static __device__ __forceinline__ float to_f(uint8_t v) { return (float)v; }
+  static __device__ __forceinline__ uint8_t from_f(float v) {
+    return (uint8_t)__float2uint_rz(fminf(__fadd_rn(v, 0.5f), 255.0f));
+  }
+};
 template <> struct Storage<float> {
   static __device__ __forceinline__ float load(const float *p) { return __ldg(p); }
   static __device__ __forceinline__ float to_f(float v) { return v; }
@@ -189,6 +198,16 @@ template <> struct Vec16<__nv_bfloat16> {
       f[2 * i] = __uint_as_float(w[i] << 16);
       f[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
     }
+  }
+};
+template <> struct Vec16<uint8_t> {
+  static constexpr int N = 16;
+  static __device__ __forceinline__ void unpack(uint4 v, float *f) {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) f[4 * i + b] = (float)((w[i] >> (8 * b)) & 0xffu);
   }
 };
 template <> struct Vec16<__half> {

@@ -11,6 +11,7 @@ HGB_INSTANTIATE_GENERIC(float, __nv_bfloat16)
 HGB_INSTANTIATE_GENERIC(float, __half)
 HGB_INSTANTIATE_GENERIC(__nv_bfloat16, float)
 HGB_INSTANTIATE_GENERIC(__half, float)
+HGB_INSTANTIATE_GENERIC(uint8_t, float)
 
 int num_tile_cfgs() { return 3; }
 
@@ -33,6 +34,7 @@ int run_conv(int dti, int dto, const ConvParams &p, int k_w, int k_h, int batch,
   if (dti == HGB_F32 && dto == HGB_F32) return run_conv_typed<float, float>(p, k_w, k_h, batch, st, key);
   if (dti == HGB_BF16 && dto == HGB_BF16) return run_conv_typed<__nv_bfloat16, __nv_bfloat16>(p, k_w, k_h, batch, st, key);
   if (dti == HGB_F16 && dto == HGB_F16) return run_conv_typed<__half, __half>(p, k_w, k_h, batch, st, key);
+  if (dti == HGB_U8 && dto == HGB_U8) return run_conv_typed<uint8_t, uint8_t>(p, k_w, k_h, batch, st, key);
   return set_error(HGB_ERR_UNSUPPORTED, "conv: storage pair without a fast kernel");
 }
 
@@ -46,6 +48,8 @@ int run_generic(int dti, int dto, const GenParams &g, int batch, cudaStream_t st
   HGB_G(HGB_F32, HGB_F16, float, __half)
   HGB_G(HGB_BF16, HGB_F32, __nv_bfloat16, float)
   HGB_G(HGB_F16, HGB_F32, __half, float)
+  HGB_G(HGB_U8, HGB_U8, uint8_t, uint8_t)
+  HGB_G(HGB_U8, HGB_F32, uint8_t, float)
 #undef HGB_G
   return set_error(HGB_ERR_UNSUPPORTED, "local_op: unsupported storage pair");
 }
@@ -109,8 +113,9 @@ extern "C" int hgb_local_op(const hgb_view *in, const hgb_window *accw, const hg
   if (rc) return rc;
   rc = check_view(out, "out");
   if (rc) return rc;
-  HGB_REQUIRE(is_float_storage(in->dtype) && is_float_storage(out->dtype),
-              "hgb_local_op: float storage (f32, bf16, f16) expected");
+  HGB_REQUIRE((is_float_storage(in->dtype) || in->dtype == HGB_U8) &&
+                  (is_float_storage(out->dtype) || (out->dtype == HGB_U8 && in->dtype == HGB_U8)),
+              "hgb_local_op: storage must be f32, bf16, f16 or u8 (u8 output from u8 input)");
   HGB_REQUIRE(in->batch == out->batch, "hgb_local_op: batch mismatch");
   HGB_REQUIRE(mask_w >= 1 && mask_h >= 1 && mask_w <= kMaxMask && mask_h <= kMaxMask,
               "hgb_local_op: mask size must be 1..15");

@@ -7,9 +7,10 @@
 // boundary remap (lib/AST/BorderHandling.cpp:124-407).
 //
 // GB300 design: a CTA computes a TW x TH output tile.  Its input tile plus
-// halo is staged once in shared memory as FP32: for FP32 images read through
-// the whole-image accessor by one cp.async.bulk.tensor load (cells outside the
-// image, which TMA fills with zeros, are then patched with the boundary rule),
+// halo is staged once in shared memory as FP32: for FP32 and u8 images read
+// through the whole-image accessor by one cp.async.bulk.tensor load (u8 bytes
+// are widened in shared memory; cells outside the image, which TMA fills with
+// zeros, are then patched with the boundary rule),
 // otherwise with 16-byte global loads, remapping element by element only the
 // chunks that leave the accessor window.  Each thread keeps a PX x PY block of
 // outputs in registers as horizontal pairs and streams the input rows of its
@@ -63,7 +64,11 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
   constexpr int SH = TH + MH - 1;
   constexpr int CPR = SW / VI;
   static_assert(TW % VI == 0 && SW % 4 == 0 && PX % 4 == 0, "tile shape");
+  constexpr bool kTma = std::is_same<TI, float>::value || std::is_same<TI, uint8_t>::value;
+  constexpr bool kU8 = std::is_same<TI, uint8_t>::value;
   __shared__ __align__(128) float tile[SH * SW];
+  // u8: the TMA box lands here as bytes and is widened into `tile`
+  __shared__ __align__(128) uint8_t raw[kU8 ? SH * SW : 16];
   __shared__ __align__(8) uint64_t bar;
 
   const int b = blockIdx.z;
@@ -76,13 +81,13 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
 
   // ---- stage input tile + halo as FP32
   const bool interior = X0 >= ax_lo && X0 + SW <= ax_hi && Y0 >= ay_lo && Y0 + SH <= ay_hi;
-  if (std::is_same<TI, float>::value && p.use_tma) {
+  if (kTma && p.use_tma) {
     // the accessor window is the whole image: one TMA load of the box
     if (threadIdx.x == 0) {
       mbar_init(&bar, 1);
       mbar_fence_init();
-      mbar_expect_tx(&bar, SH * SW * 4);
-      tma_load_3d(tile, &p.map, X0, Y0, b, &bar);
+      mbar_expect_tx(&bar, SH * SW * (int)sizeof(TI));
+      tma_load_3d(kU8 ? (void *)raw : (void *)tile, &p.map, X0, Y0, b, &bar);
     }
     __syncthreads();
     if (!mbar_wait(&bar, 0)) {
@@ -91,6 +96,20 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
         mbar_wait(&bar, 0);  // the load may still land: wait once more (bounded) before leaving
       }
       return;
+    }
+    if constexpr (kU8) {
+      // widen 4 bytes at a time: a byte b placed in the mantissa of 2^23 gives
+      // 2^23 + b exactly, and subtracting 2^23 leaves b
+      const f2 k23 = f2_pack(8388608.0f, 8388608.0f);
+      for (int c = threadIdx.x; c < SH * SW / 4; c += NT) {
+        const uint32_t w = reinterpret_cast<const uint32_t *>(raw)[c];
+        const f2 lo = f2_sub(f2_pack(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440)),
+                                     __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7441))), k23);
+        const f2 hi = f2_sub(f2_pack(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7442)),
+                                     __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7443))), k23);
+        reinterpret_cast<float4 *>(tile)[c] = make_float4(f2_lo(lo), f2_hi(lo), f2_lo(hi), f2_hi(hi));
+      }
+      if (!interior) __syncthreads();  // the patch below overwrites widened cells
     }
     if (!interior) {
       // cells outside the image (zero-filled by TMA): left / right columns, top / bottom rows
@@ -225,6 +244,15 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
 #pragma unroll
         for (int q = 0; q < PX; q += 4)
           *reinterpret_cast<float4 *>(dst + q) = make_float4(acc[oy][q], acc[oy][q + 1], acc[oy][q + 2], acc[oy][q + 3]);
+      } else if constexpr (sizeof(TO) == 1) {
+#pragma unroll
+        for (int q = 0; q < PX; q += 4) {
+          const uint32_t wv = (uint32_t)Storage<TO>::from_f(acc[oy][q]) |
+                              ((uint32_t)Storage<TO>::from_f(acc[oy][q + 1]) << 8) |
+                              ((uint32_t)Storage<TO>::from_f(acc[oy][q + 2]) << 16) |
+                              ((uint32_t)Storage<TO>::from_f(acc[oy][q + 3]) << 24);
+          *reinterpret_cast<uint32_t *>(dst + q) = wv;
+        }
       } else {
 #pragma unroll
         for (int q = 0; q < PX; q += 4) {

@@ -1,5 +1,5 @@
 // local_op_kernels.cuh -- launchers and the general-path kernel; included by
-// the per-storage-type translation units (local_op_f32.cu, _bf16.cu, _f16.cu).
+// the per-storage-type translation units (lop_sq_*_{f32,bf16,f16,u8}.cu, lop_line_*.cu).
 #pragma once
 
 #include "local_op.cuh"
@@ -18,12 +18,14 @@ int launch_cfg(const ConvParams &p0, int batch, cudaStream_t st) {
   constexpr int RX = MW / 2, VI = Vec16<TI>::N;
   constexpr int SW = round_up(RX, VI) + TW + round_up(MW - 1 - RX, VI), SH = TH + MH - 1;
   ConvParams p = p0;
-  // FP32 images read through the whole-image accessor stage their tiles with TMA
+  // FP32 and u8 images read through the whole-image accessor stage their tiles
+  // with TMA (the box origin X0 = i0 - round_up(RX, VI) is a multiple of 16 bytes)
+  constexpr bool kU8 = std::is_same<TI, uint8_t>::value;
   p.use_tma = 0;
-  if (std::is_same<TI, float>::value && p.acc_ox == 0 && p.acc_oy == 0 && p.acc_w == p.in_w && p.acc_h == p.in_h &&
-      tma_legal(p.in, p.in_pitch, p.in_bstride, batch) &&
-      make_tensor_map_3d(&p.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p.in, p.in_w, p.in_h, batch, p.in_pitch,
-                         p.in_bstride, SW, SH) == HGB_OK) {
+  if ((std::is_same<TI, float>::value || kU8) && p.acc_ox == 0 && p.acc_oy == 0 && p.acc_w == p.in_w &&
+      p.acc_h == p.in_h && tma_legal(p.in, p.in_pitch, p.in_bstride, batch) &&
+      make_tensor_map_3d(&p.map, kU8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                         (int)sizeof(TI), p.in, p.in_w, p.in_h, batch, p.in_pitch, p.in_bstride, SW, SH) == HGB_OK) {
     p.use_tma = 1;
     p.status = device_status_word();
   }

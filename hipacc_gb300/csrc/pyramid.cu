@@ -49,7 +49,7 @@ constexpr int PY_SW = PY_TW + 12, PY_SH = PY_TH + 12;        // staged G_l regio
 // TMA box of the staged region: its x origin is rounded down to a multiple of
 // 4 floats (16 bytes), so the box is 4 floats wider than the region bound
 constexpr int PY_BW = PY_SW + 4, PY_BH = PY_SH;
-constexpr int PY_THREADS = 256;
+constexpr int PY_THREADS = 256;  // five CTAs per SM (48 registers): measured faster than four at 61
 
 struct LevelMeta {
   float *g;    // Gaussian level
@@ -112,6 +112,53 @@ __device__ __forceinline__ LfTap lf_tap(float s, int x, int n, int origin) {
   return t;
 }
 
+// Five consecutive staged values of a row: two 8-byte loads and one 4-byte
+// load, the 4-byte one first when the row position is odd.
+template <bool ODD>
+__device__ __forceinline__ void load5(const float *row, float v[5]) {
+  if (ODD) {
+    v[0] = row[0];
+    const float2 a = *reinterpret_cast<const float2 *>(row + 1), b = *reinterpret_cast<const float2 *>(row + 3);
+    v[1] = a.x; v[2] = a.y; v[3] = b.x; v[4] = b.y;
+  } else {
+    const float2 a = *reinterpret_cast<const float2 *>(row), b = *reinterpret_cast<const float2 *>(row + 2);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    v[4] = row[4];
+  }
+}
+
+// 5x5 blur at two samples of one column whose top rows are D apart: rows
+// 0..D+4 of `src` are read once; each sample's 25 taps stay row-major fused
+// multiply-adds (the reference's order).
+template <int D, bool ODD>
+__device__ __forceinline__ void blur_pair(const float *mask, const float *src, float &a0, float &a1) {
+  float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+  for (int R = 0; R < D + 5; ++R) {
+    float v[5];
+    load5<ODD>(src + R * PY_BW, v);
+    if (R < 5) {
+#pragma unroll
+      for (int mx = 0; mx < 5; ++mx) s0 = __fmaf_rn(mask[R * 5 + mx], v[mx], s0);
+    }
+    if (R >= D) {
+#pragma unroll
+      for (int mx = 0; mx < 5; ++mx) s1 = __fmaf_rn(mask[(R - D) * 5 + mx], v[mx], s1);
+    }
+  }
+  a0 = s0;
+  a1 = s1;
+}
+
+__device__ __forceinline__ float blur_one(const float *mask, const float *src) {
+  float acc = 0.0f;
+#pragma unroll
+  for (int my = 0; my < 5; ++my)
+#pragma unroll
+    for (int mx = 0; mx < 5; ++mx) acc = __fmaf_rn(mask[my * 5 + mx], src[my * PY_BW + mx], acc);
+  return acc;
+}
+
 // One 64 x 32 tile of L_level (and the owned part of G_{level+1}).
 // `bar` is the CTA's mbarrier and `phase` its next phase parity.
 __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, float *gt, LfTap *cols, LfTap *rows,
@@ -156,28 +203,31 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
   }
   if (bx0 < 0 || bx0 + PY_BW > wl || ry0 < 0 || ry0 + PY_BH > hl) {
     // box cells outside the level (zero-filled by TMA) through the boundary
-    // remap: left / right columns, top / bottom rows
-    const int nl = max(0, min(PY_BW, -bx0)), rs = max(0, min(PY_BW, wl - bx0));
-    const int nt = max(0, min(PY_BH, -ry0)), bs = max(0, min(PY_BH, hl - ry0));
-    const int ncl = nl * PY_BH, ncr = (PY_BW - rs) * PY_BH, nrt = nt * PY_BW, nrb = (PY_BH - bs) * PY_BW;
+    // remap: left / right columns, top / bottom rows.  The tile reads at most
+    // two columns (rows) past the level's last one (the blur's reach from the
+    // last nearest-neighbour position w_l - 1), so the patch stops there.
+    const int cw = min(PY_BW, wl + 2 - bx0), ch = min(PY_BH, hl + 2 - ry0);  // box part the tile reads
+    const int nl = max(0, min(cw, -bx0)), rs = max(0, min(cw, wl - bx0));
+    const int nt = max(0, min(ch, -ry0)), bs = max(0, min(ch, hl - ry0));
+    const int ncl = nl * ch, ncr = (cw - rs) * ch, nrt = nt * cw, nrb = (ch - bs) * cw;
     for (int c = threadIdx.x; c < ncl + ncr + nrt + nrb; c += PY_THREADS) {
       int r, q;
       if (c < ncl) {
         r = c / nl;
         q = c - r * nl;
       } else if (c < ncl + ncr) {
-        const int d = c - ncl, n = PY_BW - rs;
+        const int d = c - ncl, n = cw - rs;
         r = d / n;
         q = rs + (d - r * n);
       } else if (c < ncl + ncr + nrt) {
         const int d = c - ncl - ncr;
-        r = d / PY_BW;
-        q = d - r * PY_BW;
+        r = d / cw;
+        q = d - r * cw;
       } else {
         const int d = c - ncl - ncr - nrt;
-        const int rr = d / PY_BW;
+        const int rr = d / cw;
         r = bs + rr;
-        q = d - rr * PY_BW;
+        q = d - rr * cw;
       }
       const int yy = remap(p.bmode, ry0 + r, 0, hl), xx = remap(p.bmode, bx0 + q, 0, wl);
       stage[r * PY_BW + q] = (yy == (int)0x80000000 || xx == (int)0x80000000)
@@ -186,48 +236,74 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
     }
     __syncthreads();
   }
-  // ---- G_{l+1} on the tile + halo: blur at the nearest-neighbour positions
+  // ---- G_{l+1} on the tile + halo: blur at the nearest-neighbour positions,
+  // two vertically adjacent samples per thread (they share 3 of their 5 rows
+  // when their G_l rows are 2 apart, 2 when 3 apart)
   const int gw = gx1 - gx0, gh = gy1 - gy0;
-  for (int c = threadIdx.x; c < PY_GW * PY_GH; c += PY_THREADS) {
-    const int r = c / PY_GW, q = c - r * PY_GW;  // constant divisor
-    if (q >= gw || r >= gh) continue;
-    const int xp = gx0 + q, yp = gy0 + r;
-    const int cx = nn(Sx, xp, wl) - 2 - rx0 + ox, cy = nn(Sy, yp, hl) - 2 - ry0;
-    const float *src = stage + cy * PY_BW + cx;
-    float acc = 0.0f;
-#pragma unroll
-    for (int my = 0; my < 5; ++my)
-#pragma unroll
-      for (int mx = 0; mx < 5; ++mx) acc = __fmaf_rn(p.mask[my * 5 + mx], src[my * PY_BW + mx], acc);
-    gt[r * PY_GW + q] = acc;
+  const int ownx0 = t.x0 / 2, owny0 = t.y0 / 2;
+  auto put = [&](int q, int r, float v) {
+    gt[r * PY_GW + q] = v;
     // owned pixels of G_{l+1}: x' in [x0/2, x0/2 + TW/2), y' likewise
-    if (xp >= t.x0 / 2 && xp < t.x0 / 2 + PY_TW / 2 && yp >= t.y0 / 2 && yp < t.y0 / 2 + PY_TH / 2)
-      __stwb(B.g + (int64_t)yp * B.pitch + xp, acc);
+    const int xp = gx0 + q, yp = gy0 + r;
+    if (xp >= ownx0 && xp < ownx0 + PY_TW / 2 && yp >= owny0 && yp < owny0 + PY_TH / 2)
+      __stwb(B.g + (int64_t)yp * B.pitch + xp, v);
+  };
+  for (int c = threadIdx.x; c < PY_GW * (PY_GH / 2); c += PY_THREADS) {
+    const int r2 = c / PY_GW, q = c - r2 * PY_GW;  // constant divisor
+    const int r = 2 * r2;
+    if (q >= gw || r >= gh) continue;
+    const int cx = nn(Sx, gx0 + q, wl) - 2 - rx0 + ox;
+    const int cy0 = nn(Sy, gy0 + r, hl) - 2 - ry0;
+    const bool two = r + 1 < gh;
+    const int d = two ? nn(Sy, gy0 + r + 1, hl) - 2 - ry0 - cy0 : 0;
+    const float *src = stage + cy0 * PY_BW + cx;
+    float a0, a1 = 0.0f;
+    if (d == 2) {
+      if (cx & 1) blur_pair<2, true>(p.mask, src, a0, a1); else blur_pair<2, false>(p.mask, src, a0, a1);
+    } else if (d == 3) {
+      if (cx & 1) blur_pair<3, true>(p.mask, src, a0, a1); else blur_pair<3, false>(p.mask, src, a0, a1);
+    } else {
+      a0 = blur_one(p.mask, src);
+      if (two) a1 = blur_one(p.mask, src + d * PY_BW);
+    }
+    put(q, r, a0);
+    if (two) put(q, r + 1, a1);
   }
   __syncthreads();
-  // ---- L_l = G_l - LF(G_{l+1}): a thread per column, rows strided
-  const int tx = threadIdx.x % PY_TW;
-  const int x = t.x0 + tx;
+  // ---- L_l = G_l - LF(G_{l+1}): a thread per pair of columns, rows strided;
+  // the two columns' arithmetic as packed FP32 (per-lane rounding unchanged)
+  const int tx = threadIdx.x % (PY_TW / 2);
+  const int x = t.x0 + 2 * tx;
   if (x < wl) {
-    const LfTap cx = cols[tx];
-    const float *gcol = stage + (x - rx0 + ox);
-    for (int r = threadIdx.x / PY_TW; r < PY_TH; r += PY_THREADS / PY_TW) {
+    const LfTap c0 = cols[2 * tx], c1 = cols[2 * tx + 1];
+    const f2 cg = f2_pack(c0.g, c1.g), cf = f2_pack(c0.f, c1.f);
+    const float *gcol = stage + (x - rx0 + ox);  // even: x and bx0 are even
+    const bool pair = x + 1 < wl;
+#pragma unroll 1
+    for (int r = threadIdx.x / (PY_TW / 2); r < PY_TH; r += PY_THREADS / (PY_TW / 2)) {
       const int y = t.y0 + r;
       if (y >= hl) break;
       const LfTap cy = rows[r];
-      const float wa = __fmul_rn(cx.g, cy.g), wb = __fmul_rn(cx.f, cy.g);
-      const float wc = __fmul_rn(cx.g, cy.f), wd = __fmul_rn(cx.f, cy.f);
-      float lf = __fmul_rn(wa, gt[cy.a * PY_GW + cx.a]);
-      lf = __fmaf_rn(wb, gt[cy.a * PY_GW + cx.c], lf);
-      lf = __fmaf_rn(wc, gt[cy.c * PY_GW + cx.a], lf);
-      lf = __fmaf_rn(wd, gt[cy.c * PY_GW + cx.c], lf);
-      __stwb(A.lap + (int64_t)y * A.pitch + x, __fsub_rn(gcol[(y - ry0) * PY_BW], lf));
+      const f2 yg = f2_pack(cy.g, cy.g), yf = f2_pack(cy.f, cy.f);
+      const f2 wa = f2_mul(cg, yg), wb = f2_mul(cf, yg), wc = f2_mul(cg, yf), wd = f2_mul(cf, yf);
+      const float *ga = gt + cy.a * PY_GW, *gc = gt + cy.c * PY_GW;
+      f2 lf = f2_mul(wa, f2_pack(ga[c0.a], ga[c1.a]));
+      lf = f2_fma(wb, f2_pack(ga[c0.c], ga[c1.c]), lf);
+      lf = f2_fma(wc, f2_pack(gc[c0.a], gc[c1.a]), lf);
+      lf = f2_fma(wd, f2_pack(gc[c0.c], gc[c1.c]), lf);
+      const float2 g = *reinterpret_cast<const float2 *>(gcol + (y - ry0) * PY_BW);
+      const f2 v = f2_sub(f2_pack(g.x, g.y), lf);
+      float *dst = A.lap + (int64_t)y * A.pitch + x;
+      if (pair)
+        __stwb(reinterpret_cast<float2 *>(dst), make_float2(f2_lo(v), f2_hi(v)));
+      else
+        __stwb(dst, f2_lo(v));
     }
   }
   return true;
 }
 
-__global__ void __launch_bounds__(PY_THREADS) pyr_level_kernel(const __grid_constant__ PyrParams p, int first) {
+__global__ void __launch_bounds__(PY_THREADS, 5) pyr_level_kernel(const __grid_constant__ PyrParams p, int first) {
   __shared__ __align__(128) float stage[PY_BW * PY_BH];
   __shared__ float gt[PY_GW * PY_GH];
   __shared__ LfTap cols[PY_TW], rows[PY_TH];
@@ -241,7 +317,7 @@ __global__ void __launch_bounds__(PY_THREADS) pyr_level_kernel(const __grid_cons
   pyr_tile(p, p.tiles[first + blockIdx.x], stage, gt, cols, rows, &bar, phase, false);
 }
 
-__global__ void __launch_bounds__(PY_THREADS) pyr_persistent_kernel(const __grid_constant__ PyrParams p) {
+__global__ void __launch_bounds__(PY_THREADS, 5) pyr_persistent_kernel(const __grid_constant__ PyrParams p) {
   __shared__ __align__(128) float stage[PY_BW * PY_BH];
   __shared__ float gt[PY_GW * PY_GH];
   __shared__ LfTap cols[PY_TW], rows[PY_TH];

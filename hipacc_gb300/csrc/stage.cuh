@@ -62,6 +62,12 @@ __device__ __forceinline__ void store_row(TO *dst, const float *v, int i, int is
     if constexpr (sizeof(TO) == 4) {
 #pragma unroll
       for (int q = 0; q < PX; q += 4) *reinterpret_cast<float4 *>(dst + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+    } else if constexpr (sizeof(TO) == 1) {
+#pragma unroll
+      for (int q = 0; q < PX; q += 4)
+        *reinterpret_cast<uint32_t *>(dst + q) =
+            (uint32_t)Storage<TO>::from_f(v[q]) | ((uint32_t)Storage<TO>::from_f(v[q + 1]) << 8) |
+            ((uint32_t)Storage<TO>::from_f(v[q + 2]) << 16) | ((uint32_t)Storage<TO>::from_f(v[q + 3]) << 24);
     } else {
 #pragma unroll
       for (int q = 0; q < PX; q += 4) {

@@ -182,7 +182,10 @@ HGB_API int hgb_graph_destroy(hgb_graph *graph);
  * cells) otherwise; both may be given (mask(dom) * input(dom)).  The fold is
  * row-major from get_init(reduce) (lib/AST/Convolution.cpp:90-100), SUM as
  * fused multiply-add.  Boundary remap per lib/AST/BorderHandling.cpp:41-407.
- * in/out: f32, bf16 or f16 storage (same or different), FP32 arithmetic.
+ * in/out: f32, bf16 or f16 storage (same or different), or u8 in with u8 or
+ * f32 out; FP32 arithmetic.  u8 results are written as the image samples'
+ * (uchar)(v + 0.5f) (samples-public/1_Local_Operators/Gaussian_Blur/src/main.cpp),
+ * saturated to [0, 255].
  * mask_w, mask_h <= 15; `mask` / `domain` are host arrays (mask_h rows of
  * mask_w); `mask_dev` (may replace `mask`) is a device array read at launch.
  * in->batch == out->batch images are processed in one launch. */

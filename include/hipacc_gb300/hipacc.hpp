@@ -11,7 +11,8 @@
 // reference's constructor arguments and member calls and run the
 // hand-written sm_103a kernels of libhipacc_gb300.so through its C ABI
 // (include/hipacc_gb300.h):
-//   Convolution<T>      Kernel::convolve(Mask, Reduce, mask()*input(mask))
+//   Convolution<T>      Kernel::convolve(Mask, Reduce, mask()*input(mask));
+//                       T = uchar writes (uchar)(result + 0.5f), saturated
 //   DomainReduce<T>     Kernel::reduce(Domain, Reduce, input(dom))
 //   Separable<T>        the 1xK + Kx1 pair of convolutions, fused
 //   BilateralFilter<T>  the bilateral sample's iterate(Domain, ...) body
