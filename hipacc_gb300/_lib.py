@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libhipacc_gb300.so")
 
 # hgb_status
-OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_ALLOC, ERR_TIMEOUT, ERR_LIMIT = range(7)
+OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_ALLOC, ERR_TIMEOUT, ERR_LIMIT, ERR_INTERNAL = range(8)
 # hgb_dtype
 U8, U8X4, I16, U16, I32, U32, U64, F16, BF16, F32, F64 = range(11)
 DTYPE_SIZE = {U8: 1, U8X4: 4, I16: 2, U16: 2, I32: 4, U32: 4, U64: 8, F16: 2, BF16: 2, F32: 4, F64: 8}

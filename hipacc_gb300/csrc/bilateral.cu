@@ -6,12 +6,16 @@
 //   out = p / d
 // with a float range sigma and a float result.
 //
-// The filter is bound by the exponential unit (one exponential per tap and
-// pixel), not by HBM.  The weight is evaluated as one base-2 exponential with
-// the spatial weight folded into the exponent,
-//   s = exp2(k2 * diff^2 + log2(mask)),  k2 = -c_r * log2(e),
-// (mask cells of 0 give log2 = -inf, i.e. s = 0, which is the Domain's skip).
-// The FP32 path uses the ex2.approx instruction through exp2f's fast form.
+// The filter is bound by arithmetic (one exponential and four FP32 lane
+// operations per tap and pixel), not by HBM.  The weight is one base-2
+// exponential with the spatial weight folded into the exponent; the staged
+// tile is pre-scaled by q = sqrt(c_r * log2(e)), so that the exponent of a
+// tap is a single fused multiply-add of the scaled difference d':
+//   s = exp2(-(d'^2 + nl)),  nl = -log2(mask)
+// (mask cells of 0 give nl = +inf, i.e. s = 0, which is the Domain's skip),
+// and out = (sum s * v') / (sum s) / q.  The FP32 path evaluates the
+// differences and the two sums for two pixels per packed f32x2 operation and
+// the exponential with ex2.approx (32 per clock and SM on this part).
 // For BF16 / F16 storage the fast path (flags bit 0) evaluates two taps'
 // weights per instruction with packed half precision (h2exp2) and keeps every
 // accumulation in FP32; its error against FP64 is stated by the tests.
@@ -34,6 +38,7 @@ struct BilParams {
   float cval;
   int vec_in, vec_out;
   float k2;                         // -c_r * log2(e)
+  float q, inv_q;                   // sqrt(-k2) and 1 / q: the FP32 path's tile scale
   float lmask[kBilMax * kBilMax];   // log2(mask), -inf for zero cells
 };
 
@@ -55,6 +60,7 @@ __device__ __forceinline__ float fast_exp2(float x) {
   return y;
 }
 
+
 template <typename T, int S, bool FAST>
 __global__ void __launch_bounds__(BL_BX *BL_BY) bilateral_kernel(const __grid_constant__ BilParams p) {
   using SH_ = BilShape<T, S>;
@@ -65,16 +71,29 @@ __global__ void __launch_bounds__(BL_BX *BL_BY) bilateral_kernel(const __grid_co
   stage_tile<T, SW, SH, BL_BX * BL_BY>(tile, p.in + (int64_t)b * p.in_bstride, p.in_pitch, i0 - HL, j0 - R, 0, p.w,
                                         0, p.h, p.bmode, p.cval, p.vec_in);
   __syncthreads();
+  if constexpr (!FAST) {
+    // the FP32 path works on values scaled by q
+    for (int c = threadIdx.x; c < SH * SW; c += BL_BX * BL_BY) tile[c] = __fmul_rn(tile[c], p.q);
+    __syncthreads();
+  }
   const int tx = threadIdx.x % BL_BX, ty = threadIdx.x / BL_BX;
   constexpr int OFF = (HL - R) % 4;
   constexpr int NV = cdiv(OFF + BL_PX + S - 1, 4);
   const int cb = HL - R - OFF + tx * BL_PX;
   float ctr[BL_PX], d[BL_PX], pp[BL_PX];
+  // FP32 path: two pixels per f32x2 lane pair
+  f2 C2[BL_PX / 2], D2[BL_PX / 2], P2[BL_PX / 2];
 #pragma unroll
   for (int px = 0; px < BL_PX; ++px) {
     ctr[px] = tile[(ty + R) * SW + HL + tx * BL_PX + px];
     d[px] = 0.0f;
     pp[px] = 0.0f;
+  }
+#pragma unroll
+  for (int k = 0; k < BL_PX / 2; ++k) {
+    C2[k] = f2_pack(ctr[2 * k], ctr[2 * k + 1]);
+    D2[k] = 0ull;
+    P2[k] = 0ull;
   }
 #pragma unroll 1
   for (int my = 0; my < S; ++my) {
@@ -89,16 +108,26 @@ __global__ void __launch_bounds__(BL_BX *BL_BY) bilateral_kernel(const __grid_co
       win[4 * v + 3] = t.w;
     }
     if constexpr (!FAST) {
+      // window pairs starting at even (E) and odd (O) positions
+      f2 E[NV * 2], O[NV * 2];
+#pragma unroll
+      for (int j = 0; j < NV * 2; ++j) {
+        E[j] = f2_pack(win[2 * j], win[2 * j + 1]);
+        O[j] = f2_pack(win[2 * j + 1], 2 * j + 2 < NV * 4 ? win[2 * j + 2] : 0.0f);
+      }
 #pragma unroll
       for (int mx = 0; mx < S; ++mx) {
-        const float lm = p.lmask[my * S + mx];
+        const float nl = -p.lmask[my * S + mx];
+        const f2 NL = f2_pack(nl, nl);
 #pragma unroll
-        for (int px = 0; px < BL_PX; ++px) {
-          const float v = win[OFF + px + mx];
-          const float df = v - ctr[px];
-          const float s = fast_exp2(__fmaf_rn(p.k2 * df, df, lm));
-          d[px] += s;
-          pp[px] = __fmaf_rn(s, v, pp[px]);
+        for (int k = 0; k < BL_PX / 2; ++k) {
+          const int st = OFF + 2 * k + mx;  // window position of the pair's first pixel
+          const f2 V = (st & 1) ? O[st >> 1] : E[st >> 1];
+          const f2 df = f2_sub(V, C2[k]);
+          const f2 t = f2_fma(df, df, NL);  // d'^2 - lm (measured faster than scalar lm - d'^2)
+          const f2 sw = f2_pack(fast_exp2(-f2_lo(t)), fast_exp2(-f2_hi(t)));
+          D2[k] = f2_add(D2[k], sw);
+          P2[k] = f2_fma(sw, V, P2[k]);
         }
       }
     } else {
@@ -125,8 +154,16 @@ __global__ void __launch_bounds__(BL_BX *BL_BY) bilateral_kernel(const __grid_co
     }
   }
   float res[BL_PX];
+  if constexpr (!FAST) {
 #pragma unroll
-  for (int px = 0; px < BL_PX; ++px) res[px] = __fdiv_rn(pp[px], d[px]);
+    for (int k = 0; k < BL_PX / 2; ++k) {
+      res[2 * k] = __fmul_rn(__fdiv_rn(f2_lo(P2[k]), f2_lo(D2[k])), p.inv_q);
+      res[2 * k + 1] = __fmul_rn(__fdiv_rn(f2_hi(P2[k]), f2_hi(D2[k])), p.inv_q);
+    }
+  } else {
+#pragma unroll
+    for (int px = 0; px < BL_PX; ++px) res[px] = __fdiv_rn(pp[px], d[px]);
+  }
   const int i = i0 + tx * BL_PX, j = j0 + ty;
   if (j < p.h && i < p.w)
     store_row<T, BL_PX>(reinterpret_cast<T *>(p.out + (int64_t)b * p.out_bstride + (int64_t)j * p.out_pitch) + i, res, i,
@@ -190,6 +227,8 @@ extern "C" int hgb_bilateral(const hgb_view *in, const hgb_view *out, const floa
   p.vec_out = ((uintptr_t)out->data % 16 == 0) && out->pitch % 16 == 0 && (out->batch == 1 || out->batch_stride % 16 == 0);
   const double c_r = 0.5 / ((double)sigma_r * (double)sigma_r);
   p.k2 = (float)(-c_r * 1.4426950408889634);  // log2(e)
+  p.q = (float)std::sqrt(c_r * 1.4426950408889634);
+  p.inv_q = (float)(1.0 / std::sqrt(c_r * 1.4426950408889634));
   for (int i = 0; i < size * size; ++i)
     p.lmask[i] = smask[i] > 0.0f ? (float)std::log2((double)smask[i]) : -INFINITY;
   for (int i = 0; i < size * size; ++i)

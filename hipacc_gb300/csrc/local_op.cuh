@@ -89,8 +89,7 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
       mbar_expect_tx(&bar, SH * SW * (int)sizeof(TI));
       tma_load_3d(kU8 ? (void *)raw : (void *)tile, &p.map, X0, Y0, b, &bar);
     }
-    __syncthreads();
-    if (!mbar_wait(&bar, 0)) {
+    if (!cta_wait(&bar, 0)) {
       if (threadIdx.x == 0) {
         record_status(p.status, HGB_ERR_TIMEOUT);
         mbar_wait(&bar, 0);  // the load may still land: wait once more (bounded) before leaving

@@ -347,8 +347,7 @@ __global__ void __launch_bounds__(GB_T) gray_bulk_kernel(const __grid_constant__
       mbar_expect_tx(&bar, GB_STAGE);
       bulk_load(stage, p.in + u * GB_STAGE, GB_STAGE, &bar);
     }
-    __syncthreads();
-    if (!mbar_wait(&bar, 0)) {
+    if (!cta_wait(&bar, 0)) {
       if (threadIdx.x == 0) {
         record_status(B.status, HGB_ERR_TIMEOUT);
         mbar_wait(&bar, 0);  // the copy may still land: wait once more (bounded) before leaving

@@ -155,8 +155,7 @@ __global__ void __launch_bounds__(SP_BX *SP_BY) separable_kernel(const __grid_co
       mbar_expect_tx(&bar, SH * SW * (int)sizeof(T));
       tma_load_3d(tile, &p.map, X0, Y0, b, &bar);
     }
-    __syncthreads();
-    if (!mbar_wait(&bar, 0)) {
+    if (!cta_wait(&bar, 0)) {
       if (threadIdx.x == 0) {
         record_status(p.status, HGB_ERR_TIMEOUT);
         mbar_wait(&bar, 0);  // the load may still land: wait once more (bounded) before leaving

@@ -330,8 +330,7 @@ __global__ void __launch_bounds__(T_WARPS * 32) sobel3_tma_kernel(const __grid_c
     mbar_expect_tx(&bar, T_STAGE);
     tma_load_3d(tile, &P.map, i0 - 16, j0 - 1, b, &bar);
   }
-  __syncthreads();
-  if (!mbar_wait(&bar, 0)) {
+  if (!cta_wait(&bar, 0)) {
     if (threadIdx.x == 0) {
       record_status(P.status, HGB_ERR_TIMEOUT);
       mbar_wait(&bar, 0);  // the load may still land: wait once more (bounded) before leaving

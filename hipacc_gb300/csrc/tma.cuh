@@ -64,6 +64,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
   return false;
 }
 
+// One thread waits (bounded) for the barrier's phase and the CTA barrier that
+// follows orders its acquire before every thread's reads of the landed bytes;
+// the other threads sleep at the CTA barrier instead of polling the mbarrier
+// (polling warps take issue slots from the CTAs that have work).  Same result
+// on every thread: false when the wait expired.
+__device__ __forceinline__ bool cta_wait(uint64_t *bar, unsigned parity) {
+  int late = 0;
+  if (threadIdx.x == 0) late = !mbar_wait(bar, parity);
+  return !__syncthreads_or(late);
+}
+
 // order earlier generic-proxy accesses of shared memory before async-proxy
 // (TMA) writes into it
 __device__ __forceinline__ void fence_proxy_async_smem() {

@@ -40,7 +40,8 @@ typedef enum hgb_status {
   HGB_ERR_CUDA = 3,        /* a CUDA runtime call failed */
   HGB_ERR_ALLOC = 4,       /* device or host allocation failed */
   HGB_ERR_TIMEOUT = 5,     /* a bounded device-side wait expired */
-  HGB_ERR_LIMIT = 6        /* request exceeds a fixed capacity */
+  HGB_ERR_LIMIT = 6,       /* request exceeds a fixed capacity */
+  HGB_ERR_INTERNAL = 7     /* a device-side consistency check failed (a library defect) */
 } hgb_status;
 
 /* pixel storage types */
@@ -124,7 +125,8 @@ HGB_API int hgb_autotune_load(const char *path);
 
 /* Device status word: HGB_OK, or the error a kernel recorded since the last
  * call (HGB_ERR_TIMEOUT when a bounded wait on a TMA copy or an inter-tile
- * dependency expired).  Synchronises the device and clears the word. */
+ * dependency expired, HGB_ERR_INTERNAL when a kernel's consistency check
+ * failed).  Synchronises the device and clears the word. */
 HGB_API int hgb_device_status(int *status);
 
 /* Reserve the per-device workspace (reduction partials, tickets, work-lists)
