@@ -169,7 +169,7 @@ __device__ __forceinline__ float blur_one(const float *mask, const float *src) {
 // One 64 x 32 tile of L_level (and the owned part of G_{level+1}).
 // `bar` is the CTA's mbarrier and `phase` its next phase parity.
 __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, float *gt, LfTap *cols, LfTap *rows,
-                         uint64_t *bar, unsigned &phase, bool coherent) {
+                         int *ncx, int *ncy, uint64_t *bar, unsigned &phase, bool coherent) {
   // ---- stage the G_l box [by, by + BH) x [bx, bx + BW) with one TMA load
   if (threadIdx.x == 0) {
     // in the persistent form G_l was written by other CTAs of this launch
@@ -195,11 +195,21 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
   const int ry0 = nn(Sy, gy0, hl) - 2;
   // the box origin: x rounded down to a multiple of 4 floats (16 bytes)
   const int bx0 = rx0 & ~3, ox = rx0 - bx0;
-  // linear-filtering taps of the tile's columns and rows (while the box lands)
-  if (threadIdx.x < PY_TW)
-    cols[threadIdx.x] = lf_tap(sx, t.x0 + threadIdx.x, wn, gx0);
-  else if (threadIdx.x < PY_TW + PY_TH)
-    rows[threadIdx.x - PY_TW] = lf_tap(sy, t.y0 + threadIdx.x - PY_TW, hn, gy0);
+  // while the box lands: the linear-filtering taps of the tile's columns and
+  // rows, and the staged positions of the blur's nearest-neighbour samples
+  for (int i = threadIdx.x; i < PY_TW + PY_TH + PY_GW + PY_GH; i += PY_THREADS) {
+    if (i < PY_TW) {
+      cols[i] = lf_tap(sx, t.x0 + i, wn, gx0);
+    } else if (i < PY_TW + PY_TH) {
+      rows[i - PY_TW] = lf_tap(sy, t.y0 + i - PY_TW, hn, gy0);
+    } else if (i < PY_TW + PY_TH + PY_GW) {
+      const int q = i - PY_TW - PY_TH;
+      ncx[q] = nn(Sx, gx0 + q, wl) - 2 - rx0 + ox;
+    } else {
+      const int r = i - PY_TW - PY_TH - PY_GW;
+      ncy[r] = nn(Sy, gy0 + r, hl) - 2 - ry0;
+    }
+  }
   const bool landed = cta_wait(bar, phase);
   phase ^= 1u;
   if (!landed) {
@@ -264,10 +274,11 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
     const int r2 = c / PY_GW, q = c - r2 * PY_GW;  // constant divisor
     const int r = 2 * r2;
     if (q >= gw || r >= gh) continue;
-    const int cx = nn(Sx, gx0 + q, wl) - 2 - rx0 + ox;
-    const int cy0 = nn(Sy, gy0 + r, hl) - 2 - ry0;
+    const int cx = ncx[q];
+    const int2 cy = *reinterpret_cast<const int2 *>(ncy + r);  // rows of samples r and r + 1 (r even)
+    const int cy0 = cy.x;
     const bool two = r + 1 < gh;
-    const int d = two ? nn(Sy, gy0 + r + 1, hl) - 2 - ry0 - cy0 : 0;
+    const int d = two ? cy.y - cy0 : 0;
     const float *src = stage + cy0 * PY_BW + cx;
     float a0, a1 = 0.0f;
     if (d == 2) {
@@ -319,6 +330,7 @@ __global__ void __launch_bounds__(PY_THREADS, 10) pyr_level_kernel(const __grid_
   __shared__ __align__(128) float stage[PY_BW * PY_BH];
   __shared__ float gt[PY_GW * PY_GH];
   __shared__ LfTap cols[PY_TW], rows[PY_TH];
+  __shared__ __align__(8) int ncx[PY_GW], ncy[PY_GH];
   __shared__ __align__(8) uint64_t bar;
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
@@ -326,13 +338,14 @@ __global__ void __launch_bounds__(PY_THREADS, 10) pyr_level_kernel(const __grid_
   }
   __syncthreads();
   unsigned phase = 0;
-  pyr_tile(p, p.tiles[first + blockIdx.x], stage, gt, cols, rows, &bar, phase, false);
+  pyr_tile(p, p.tiles[first + blockIdx.x], stage, gt, cols, rows, ncx, ncy, &bar, phase, false);
 }
 
 __global__ void __launch_bounds__(PY_THREADS, 10) pyr_persistent_kernel(const __grid_constant__ PyrParams p) {
   __shared__ __align__(128) float stage[PY_BW * PY_BH];
   __shared__ float gt[PY_GW * PY_GH];
   __shared__ LfTap cols[PY_TW], rows[PY_TH];
+  __shared__ __align__(8) int ncx[PY_GW], ncy[PY_GH];
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_t;
   __shared__ int s_ok;
@@ -369,7 +382,7 @@ __global__ void __launch_bounds__(PY_THREADS, 10) pyr_persistent_kernel(const __
     const int t = s_t;
     if (t >= p.ntiles) return;
     const PyrTile tl = p.tiles[t];
-    if (s_ok && !pyr_tile(p, tl, stage, gt, cols, rows, &bar, phase, true)) return;
+    if (s_ok && !pyr_tile(p, tl, stage, gt, cols, rows, ncx, ncy, &bar, phase, true)) return;
     __syncthreads();
     if (threadIdx.x == 0) red_release_add(&p.done[tl.img * p.levels + tl.level], 1u);
   }
