@@ -13,8 +13,8 @@
 // shared memory updated by shared-memory atomics -- for u8 pixels and up to
 // 256 bins one column per lane (a warp's 32 updates land in 32 banks),
 // otherwise one copy per warp up to 1024 bins and one copy beyond -- the
-// image read as 16-pixel chunks
-// with 16-byte loads where the layout allows, and one global atomic add per
+// image read as 16-pixel chunks with 16-byte loads where the layout allows
+// (several chunks' loads in flight per thread), and one global atomic add per
 // non-empty private bin at the end.  Integer sums, so the result does not
 // depend on the order.  u8 pixels map through a 256-entry table computed
 // with the same float arithmetic, replicated once per shared-memory bank.
@@ -74,28 +74,47 @@ __global__ void __launch_bounds__(HB_T) hist_kernel(const __grid_constant__ Hist
   const int64_t rows = p.dense ? 1 : (int64_t)p.h * p.batch;
   const int64_t cpr = (row_len + 15) / 16;
   const int64_t items = rows * cpr;
-  for (int64_t it = (int64_t)blockIdx.x * HB_T + threadIdx.x; it < items; it += (int64_t)gridDim.x * HB_T) {
-    const int64_t row = it / cpr, chunk = it - row * cpr;
-    const char *base;
-    if (p.dense) {
-      base = p.in + ((int64_t)p.oy * p.pitch + (int64_t)p.ox * p.es);
-    } else {
-      const int b = (int)(row / p.h), y = (int)(row - (int64_t)b * p.h);
-      base = p.in + (int64_t)b * p.bstride + (int64_t)(p.oy + y) * p.pitch + (int64_t)p.ox * p.es;
+  // U chunks per thread and pass, all loads issued before the updates (more
+  // bytes in flight per SM: a resident wave holds few CTAs)
+  constexpr int NV = 16 * sizeof(T) / 16;
+  constexpr int U = sizeof(T) == 1 ? 4 : 2;
+  const int64_t stride = (int64_t)gridDim.x * HB_T;
+  for (int64_t it0 = (int64_t)blockIdx.x * HB_T + threadIdx.x; it0 < items; it0 += U * stride) {
+    uint4 v[U][NV];
+    const T *src[U];
+    int n[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t it = it0 + u * stride;
+      n[u] = 0;
+      src[u] = nullptr;
+      if (it < items) {
+        const int64_t row = it / cpr, chunk = it - row * cpr;
+        const char *base;
+        if (p.dense) {
+          base = p.in + ((int64_t)p.oy * p.pitch + (int64_t)p.ox * p.es);
+        } else {
+          const int b = (int)(row / p.h), y = (int)(row - (int64_t)b * p.h);
+          base = p.in + (int64_t)b * p.bstride + (int64_t)(p.oy + y) * p.pitch + (int64_t)p.ox * p.es;
+        }
+        src[u] = reinterpret_cast<const T *>(base) + chunk * 16;
+        const int64_t left = row_len - chunk * 16;
+        n[u] = left < 16 ? (int)left : 16;
+        if (p.vec && n[u] == 16) {
+#pragma unroll
+          for (int k = 0; k < NV; ++k) v[u][k] = ldg16(reinterpret_cast<const char *>(src[u]) + 16 * k);
+        }
+      }
     }
-    const T *src = reinterpret_cast<const T *>(base) + chunk * 16;
-    const int64_t left = row_len - chunk * 16;
-    const int n = left < 16 ? (int)left : 16;
-    if (p.vec && n == 16) {
-      constexpr int NV = 16 * sizeof(T) / 16;
-      uint4 v[NV];
 #pragma unroll
-      for (int k = 0; k < NV; ++k) v[k] = ldg16(reinterpret_cast<const char *>(src) + 16 * k);
-      const T *e = reinterpret_cast<const T *>(v);
+    for (int u = 0; u < U; ++u) {
+      if (p.vec && n[u] == 16) {
+        const T *e = reinterpret_cast<const T *>(v[u]);
 #pragma unroll
-      for (int k = 0; k < 16; ++k) put(e[k]);
-    } else {
-      for (int k = 0; k < n; ++k) put(src[k]);
+        for (int k = 0; k < 16; ++k) put(e[k]);
+      } else {
+        for (int k = 0; k < n[u]; ++k) put(src[u][k]);
+      }
     }
   }
   __syncthreads();
