@@ -3,15 +3,11 @@
 #include <cstring>
 
 #include "autotune.h"
-#include "local_op_kernels.cuh"
+// declarations only: the kernels are instantiated in the lop_*.cu units, which
+// compile in parallel
+#include "local_op.cuh"
 
 namespace hgb {
-
-HGB_INSTANTIATE_GENERIC(float, __nv_bfloat16)
-HGB_INSTANTIATE_GENERIC(float, __half)
-HGB_INSTANTIATE_GENERIC(__nv_bfloat16, float)
-HGB_INSTANTIATE_GENERIC(__half, float)
-HGB_INSTANTIATE_GENERIC(uint8_t, float)
 
 int num_tile_cfgs() { return 3; }
 
