@@ -111,7 +111,8 @@ __host__ __device__ __forceinline__ int remap(int mode, int idx, int lo, int hi)
 
 template <typename T> struct Storage;
 // u8 pixels: widened exactly; written as the samples' (uchar)(x + 0.5f), with
-// values outside [0, 255] saturated (the C cast leaves them undefined)
+// values outside [0, 255] saturated (the C cast leaves them undefined; NaN
+// gives 255, as fminf returns the number)
 template <> struct Storage<uint8_t> {
   static __device__ __forceinline__ float load(const uint8_t *p) { return (float)__ldg(p); }
   static __device__ __forceinline__ float to_f(uint8_t v) { return (float)v; }

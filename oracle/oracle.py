@@ -102,6 +102,7 @@ def ref():
         R = C.CDLL(REF_PATH)
         R.ref_conv_f32.argtypes = [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    f32p]
+        R.ref_conv_u8.argtypes = [u8p, C.c_int, C.c_int, f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, u8p]
         R.ref_sobel_mag_u8.argtypes = [u8p, C.c_int, C.c_int, i32p, i32p, C.c_int, C.c_int, u8p]
         R.ref_gray_u8.argtypes = [u8p, C.c_int, C.c_int, u8p]
         R.ref_sum_u8_u64.argtypes = [u8p, C.c_int, C.c_int]
@@ -159,6 +160,24 @@ def local_op(img, mask=None, domain=None, size=None, reduce=SUM, boundary=CLAMP,
     fn(img, w, aox, aoy, aw, ah, out, iow, iox, ioy, iw, ih, _ptr(mask), _ptr(domain), mw, mh, reduce,
        boundary, const, contract, nt)
     return out
+
+
+def write_u8(v):
+    """A float result written to a u8 image as the image samples write it,
+    ``(uchar)(v + 0.5f)`` (samples-public/1_Local_Operators/Gaussian_Blur/src/main.cpp),
+    in FP32; values outside [0, 255] saturate where C leaves the cast undefined
+    (NaN gives 255: the kernels clamp with fminf, which returns the number)."""
+    s = (np.asarray(v, np.float32) + np.float32(0.5)).astype(np.float32)
+    s = np.nan_to_num(s, nan=255.0, posinf=255.0, neginf=0.0)
+    return np.clip(np.trunc(s), 0, 255).astype(np.uint8)
+
+
+def local_op_u8(img, mask=None, domain=None, size=None, reduce=SUM, boundary=CLAMP, const=0.0, contract=1, **kw):
+    """A local operator on a u8 image: the FP32 operator on the widened pixels,
+    written back with ``write_u8``."""
+    r = local_op(np.asarray(img).astype(np.float32), mask=mask, domain=domain, size=size, reduce=reduce,
+                 boundary=boundary, const=const, contract=contract, **kw)
+    return write_u8(r)
 
 
 def separable(img, row_taps, col_taps, boundary=CLAMP, const=0.0, contract=1, nthreads=0):

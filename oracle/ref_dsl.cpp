@@ -8,7 +8,9 @@
 // pin the restated oracle (hgb_oracle.cpp) and to generate tests/golden/.
 //
 // Kernel bodies mirror the sample programs:
-//   convolve:  samples-public/1_Local_Operators/Gaussian_Blur/src/main.cpp:56-61
+//   convolve:  samples-public/1_Local_Operators/Gaussian_Blur/src/main.cpp:56-61 (float and
+//              the sample's own uchar form with `+ 0.5f`)
+//   erode / dilate: samples-public/1_Local_Operators/Erode/src/main.cpp, Dilate/src/main.cpp
 //   Sobel:     samples-public/3_Preprocessing/Sobel/src/main.cpp:56-67
 //   bilateral: samples-public/3_Preprocessing/Bilateral_Filter/src/main.cpp:63-77
 //   reduction: samples-public/2_Global_Operators/Reduction_Sum/src/main.cpp:50-62
@@ -49,6 +51,36 @@ class DomRedK : public Kernel<float> {
   }
   void kernel() {
     output() = reduce(dom, mode, [&]() -> float { return in(dom); });
+  }
+};
+
+// the Gaussian-blur sample's u8 body: (uchar)(convolve(...) + 0.5f)
+class ConvU8K : public Kernel<uchar> {
+  Accessor<uchar> &in;
+  Mask<float> &mask;
+
+ public:
+  ConvU8K(IterationSpace<uchar> &it, Accessor<uchar> &in, Mask<float> &m) : Kernel(it), in(in), mask(m) {
+    add_accessor(&in);
+  }
+  void kernel() {
+    output() = (uchar)(convolve(mask, Reduce::SUM, [&]() -> float { return mask() * in(mask); }) + 0.5f);
+  }
+};
+
+// the Erode / Dilate samples' body: reduce(dom, MIN / MAX) over uchar
+class DomRedU8K : public Kernel<uchar> {
+  Accessor<uchar> &in;
+  Domain &dom;
+  Reduce mode;
+
+ public:
+  DomRedU8K(IterationSpace<uchar> &it, Accessor<uchar> &in, Domain &d, Reduce mode)
+      : Kernel(it), in(in), dom(d), mode(mode) {
+    add_accessor(&in);
+  }
+  void kernel() {
+    output() = reduce(dom, mode, [&]() -> uchar { return in(dom); });
   }
 };
 
@@ -193,6 +225,28 @@ void conv_sized(const float *in, int w, int h, const float *coef, int bmode, int
   std::memcpy(out, OUT.data(), sizeof(float) * (size_t)w * h);
 }
 
+template <int MH, int MW>
+void conv_u8_sized(const uint8_t *in, int w, int h, const float *coef, int bmode, int dom_mode, int red,
+                   uint8_t *out) {
+  float c[MH][MW];
+  std::memcpy(c, coef, sizeof(c));
+  Mask<float> mask(c);
+  Image<uchar> IN(w, h, const_cast<uchar *>(in));
+  Image<uchar> OUT(w, h);
+  BoundaryCondition<uchar> bc = make_bc(IN, mask, bmode);
+  Accessor<uchar> acc(bc);
+  IterationSpace<uchar> it(OUT);
+  if (dom_mode) {
+    Domain dom(mask);
+    DomRedU8K k(it, acc, dom, (Reduce)red);
+    k.execute();
+  } else {
+    ConvU8K k(it, acc, mask);
+    k.execute();
+  }
+  std::memcpy(out, OUT.data(), (size_t)w * h);
+}
+
 template <int S>
 void sobel_sized(const uint8_t *in, int w, int h, const int *cx, const int *cy, int bmode, uint8_t *out) {
   int ax[S][S], ay[S][S];
@@ -238,6 +292,17 @@ int ref_conv_f32(const float *in, int w, int h, const float *coef, int mw, int m
   HGB_CASE(3, 3) HGB_CASE(5, 5) HGB_CASE(7, 7) HGB_CASE(9, 9) HGB_CASE(13, 13)
   HGB_CASE(1, 3) HGB_CASE(3, 1) HGB_CASE(1, 5) HGB_CASE(5, 1) HGB_CASE(1, 9) HGB_CASE(9, 1)
   HGB_CASE(3, 5) HGB_CASE(5, 3) HGB_CASE(1, 7) HGB_CASE(7, 1) HGB_CASE(1, 13) HGB_CASE(13, 1)
+#undef HGB_CASE
+  return -1;
+}
+
+// u8 images: the Gaussian-blur sample's convolution (dom_mode 0) or the
+// Erode / Dilate samples' Domain reduction (dom_mode 1, red MIN or MAX)
+int ref_conv_u8(const uint8_t *in, int w, int h, const float *coef, int mw, int mh, int bmode, int dom_mode,
+                int red, uint8_t *out) {
+#define HGB_CASE(H, W) \
+  if (mh == H && mw == W) { conv_u8_sized<H, W>(in, w, h, coef, bmode, dom_mode, red, out); return 0; }
+  HGB_CASE(3, 3) HGB_CASE(5, 5) HGB_CASE(7, 7) HGB_CASE(1, 5) HGB_CASE(5, 1)
 #undef HGB_CASE
   return -1;
 }

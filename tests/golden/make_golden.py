@@ -117,6 +117,27 @@ def main():
             dst = np.zeros((dh, dw), np.float32)
             assert R.ref_cpu_interp_f32(m, src, sw, sh, dst, dw, dh) == 0
             out[f"interp_{name}_{sw}x{sh}_{dw}x{dh}"] = dst
+    # u8 images: the Gaussian-blur sample's (uchar)(convolve(...) + 0.5f) and
+    # the Erode / Dilate samples' reduce(dom, MIN / MAX) over uchar
+    for (mh, mw) in [(3, 3), (5, 5), (1, 5), (5, 1)]:
+        for b in (O.CLAMP, O.REPEAT, O.MIRROR, O.CONSTANT):
+            img = rng.integers(0, 256, (19, 23), dtype=np.uint8)
+            m = rng.random((mh, mw)).astype(np.float32)
+            m /= m.sum()
+            r = np.zeros_like(img)
+            assert R.ref_conv_u8(img, 23, 19, m, mw, mh, b, 0, 0, r) == 0
+            out[f"conv_u8_{mh}x{mw}_b{b}_in"] = img
+            out[f"conv_u8_{mh}x{mw}_b{b}_mask"] = m
+            out[f"conv_u8_{mh}x{mw}_b{b}_out"] = r
+    for red in (O.MIN, O.MAX):
+        img = rng.integers(0, 256, (17, 21), dtype=np.uint8)
+        dom = np.ones((3, 3), np.float32)
+        dom[0, 0] = dom[2, 2] = 0.0
+        r = np.zeros_like(img)
+        assert R.ref_conv_u8(img, 21, 17, dom, 3, 3, O.CLAMP, 1, red, r) == 0
+        out[f"domain_u8_r{red}_in"] = img
+        out[f"domain_u8_r{red}_dom"] = dom.astype(np.uint8)
+        out[f"domain_u8_r{red}_out"] = r
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path), "bytes,", len(out), "arrays")
 

@@ -30,6 +30,34 @@ def test_domain_golden(oracle, golden):
         assert np.array_equal(r, golden[k + "_out"]), k
 
 
+def test_u8_local_op_golden(oracle, golden):
+    """u8 images through the reference's DSL: the Gaussian-blur sample's
+    (uchar)(convolve + 0.5f) and the Erode / Dilate samples' reduce(dom, MIN / MAX)."""
+    O = oracle
+    n = 0
+    for (mh, mw) in [(3, 3), (5, 5), (1, 5), (5, 1)]:
+        for b in (O.CLAMP, O.REPEAT, O.MIRROR, O.CONSTANT):
+            k = f"conv_u8_{mh}x{mw}_b{b}"
+            r = O.local_op_u8(golden[k + "_in"], mask=golden[k + "_mask"], boundary=b, const=0.0, contract=0)
+            assert np.array_equal(r, golden[k + "_out"]), k
+            n += 1
+    for red in (O.MIN, O.MAX):
+        k = f"domain_u8_r{red}"
+        dom = golden[k + "_dom"]
+        r = O.local_op_u8(golden[k + "_in"], domain=dom, size=dom.shape, reduce=red, boundary=O.CLAMP, contract=0)
+        assert np.array_equal(r, golden[k + "_out"]), k
+        n += 1
+    assert n == 18
+
+
+def test_write_u8_rule(oracle):
+    """(uchar)(v + 0.5f) for in-range values; saturation outside.  The sum is
+    rounded in FP32 first: 0.49999997f + 0.5f lies halfway between 1 - 2^-24
+    and 1 and rounds to 1, as the sample's C expression does."""
+    v = np.array([0.0, 0.49999997, 0.5, 1.49, 254.5, 254.49998, 255.2, 300.0, -0.4, -3.0], np.float32)
+    assert oracle.write_u8(v).tolist() == [0, 1, 1, 1, 255, 254, 255, 255, 0, 0]
+
+
 def test_sobel_gray_reduce_golden(oracle, golden):
     O = oracle
     for b in (O.CLAMP, O.REPEAT, O.MIRROR, O.CONSTANT):
