@@ -65,6 +65,70 @@ def test_host_side_validation_without_gpu(hgb_lib):
     assert rc == L.ERR_INVALID
 
 
+def test_validation_of_storage_and_operator_arguments(hgb_lib):
+    """Storage pairs, histogram, bilateral and resampling arguments are checked on the host."""
+    from hipacc_gb300 import _lib as L
+
+    u8 = L.View(0x1000, L.U8, 16, 16, 1, 16, 256)
+    bf = L.View(0x1000, L.BF16, 16, 16, 1, 32, 512)
+    f32 = L.View(0x1000, L.F32, 16, 16, 1, 64, 1024)
+    m = (C.c_float * 9)()
+    # u8 output only from u8 input
+    rc = hgb_lib.hgb_local_op(C.byref(bf), None, C.byref(u8), None, m, None, None, 3, 3, 0, 1, 0.0, None)
+    assert rc == L.ERR_INVALID and b"u8" in hgb_lib.hgb_last_error()
+    # histogram: bin count and result buffer
+    rc = hgb_lib.hgb_histogram(C.byref(u8), None, 0, C.c_void_p(0x2000), None, None)
+    assert rc == L.ERR_INVALID and b"num_bins" in hgb_lib.hgb_last_error()
+    rc = hgb_lib.hgb_histogram(C.byref(u8), None, 16385, C.c_void_p(0x2000), None, None)
+    assert rc == L.ERR_INVALID and b"num_bins" in hgb_lib.hgb_last_error()
+    rc = hgb_lib.hgb_histogram(C.byref(u8), None, 256, None, None, None)
+    assert rc == L.ERR_INVALID and b"result" in hgb_lib.hgb_last_error()
+    rc = hgb_lib.hgb_histogram(C.byref(bf), None, 256, C.c_void_p(0x2000), None, None)
+    assert rc == L.ERR_INVALID
+    # bilateral: odd sizes 3..13, positive sigma, non-negative weights, same storage
+    sm = (C.c_float * 169)(*([0.5] * 169))
+    for size, sigma in ((4, 0.1), (15, 0.1), (5, 0.0)):
+        rc = hgb_lib.hgb_bilateral(C.byref(f32), C.byref(f32), sm, size, sigma, 1, 0.0, 0, None)
+        assert rc == L.ERR_INVALID, (size, sigma)
+    rc = hgb_lib.hgb_bilateral(C.byref(f32), C.byref(bf), sm, 5, 0.1, 1, 0.0, 0, None)
+    assert rc == L.ERR_INVALID
+    neg = (C.c_float * 9)(*([0.5] * 8 + [-1.0]))
+    rc = hgb_lib.hgb_bilateral(C.byref(f32), C.byref(f32), neg, 3, 0.1, 1, 0.0, 0, None)
+    assert rc == L.ERR_INVALID and b"non-negative" in hgb_lib.hgb_last_error()
+    # packed half weights need half storage
+    rc = hgb_lib.hgb_bilateral(C.byref(f32), C.byref(f32), sm, 5, 0.1, 1, 0.0, 1, None)
+    assert rc == L.ERR_INVALID
+    # resampling modes 1..5 only
+    for mode in (0, 6):
+        rc = hgb_lib.hgb_resample(C.byref(f32), C.byref(f32), mode, None)
+        assert rc == L.ERR_INVALID and b"imode" in hgb_lib.hgb_last_error()
+
+
+def test_autotune_cache_persistence(hgb_lib, tmp_path):
+    """The tile-configuration cache round-trips through its JSON file (host only)."""
+    from hipacc_gb300 import _lib as L
+
+    src = tmp_path / "tune.json"
+    src.write_text('{\n  "conv|f32|5x5|1024x1024": [1, 0.084000],\n  "conv|u8|5x5|1024x1024": [2, 0.120000]\n}\n')
+    assert hgb_lib.hgb_autotune_clear() == L.OK
+    assert hgb_lib.hgb_autotune_count() == 0
+    assert hgb_lib.hgb_autotune_load(str(src).encode()) == L.OK
+    assert hgb_lib.hgb_autotune_count() == 2
+    out = tmp_path / "saved.json"
+    assert hgb_lib.hgb_autotune_save(str(out).encode()) == L.OK
+    assert hgb_lib.hgb_autotune_clear() == L.OK and hgb_lib.hgb_autotune_count() == 0
+    assert hgb_lib.hgb_autotune_load(str(out).encode()) == L.OK
+    assert hgb_lib.hgb_autotune_count() == 2
+    text = out.read_text()
+    assert '"conv|u8|5x5|1024x1024": [2, 0.120000]' in text
+    bad = tmp_path / "bad.json"
+    bad.write_text('{"key": "no configuration here"}')
+    assert hgb_lib.hgb_autotune_load(str(bad).encode()) == L.ERR_INVALID
+    assert hgb_lib.hgb_autotune_load(str(tmp_path / "missing.json").encode()) == L.ERR_INVALID
+    assert hgb_lib.hgb_autotune_save(None) == L.ERR_INVALID
+    assert hgb_lib.hgb_autotune_clear() == L.OK
+
+
 def test_missing_library_fails_loudly(tmp_path):
     from hipacc_gb300 import _lib as L
 
