@@ -129,6 +129,20 @@ def test_autotune_cache_persistence(hgb_lib, tmp_path):
     assert hgb_lib.hgb_autotune_clear() == L.OK
 
 
+def test_python_api_rejects_host_tensors(hgb_lib):
+    """The torch binding refuses CPU tensors instead of passing host pointers to the kernels."""
+    import numpy as np
+    import torch
+
+    from hipacc_gb300 import api
+
+    x = torch.zeros((8, 8))
+    with pytest.raises(ValueError, match="CUDA tensors"):
+        api.local_op(x, torch.zeros_like(x), mask=np.ones((3, 3), np.float32))
+    with pytest.raises(ValueError, match="CUDA tensors"):
+        api.histogram(torch.zeros((8, 8), dtype=torch.uint8), 16)
+
+
 def test_missing_library_fails_loudly(tmp_path):
     from hipacc_gb300 import _lib as L
 
