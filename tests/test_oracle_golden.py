@@ -154,6 +154,22 @@ def test_live_reference_pin(oracle, b):
     r = np.zeros_like(img)
     R.ref_sobel_mag_u8(img, 52, 40, O.SOBEL3_X, O.SOBEL3_Y, 3, b, r)
     assert np.array_equal(O.sobel_mag(img, boundary=b), r)
+    # u8 images through the samples' own uchar kernels (blur with + 0.5f, erode / dilate)
+    for (mh, mw) in [(3, 3), (5, 5), (7, 7)]:
+        img = rng.integers(0, 256, (29, 37), dtype=np.uint8)
+        m = rng.random((mh, mw)).astype(np.float32)
+        m /= m.sum()
+        r = np.zeros_like(img)
+        assert R.ref_conv_u8(img, 37, 29, m, mw, mh, b, 0, 0, r) == 0
+        assert np.array_equal(O.local_op_u8(img, mask=m, boundary=b, contract=0), r)
+    for red in (O.MIN, O.MAX):
+        img = rng.integers(0, 256, (29, 37), dtype=np.uint8)
+        dom = (rng.random((5, 5)) > 0.3).astype(np.float32)
+        dom[2, 2] = 1.0
+        r = np.zeros_like(img)
+        assert R.ref_conv_u8(img, 37, 29, dom, 5, 5, b, 1, red, r) == 0
+        got = O.local_op_u8(img, domain=dom.astype(np.uint8), size=(5, 5), reduce=red, boundary=b, contract=0)
+        assert np.array_equal(got, r), red
     f = rng.random((40, 52), dtype=np.float32)
     nc = R.ref_cpu_red_cores_omp()
     assert np.float32(R.ref_cpu_red_sum_f32_omp(f, 52, 40)) == np.float32(O.reduce_f32(f, O.SUM, nc))
