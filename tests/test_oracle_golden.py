@@ -154,6 +154,13 @@ def test_live_reference_pin(oracle, b):
     r = np.zeros_like(img)
     R.ref_sobel_mag_u8(img, 52, 40, O.SOBEL3_X, O.SOBEL3_Y, 3, b, r)
     assert np.array_equal(O.sobel_mag(img, boundary=b), r)
+    # the separable form: the reference writes it as two DSL convolutions (1x9, then 9x1)
+    img = rng.random((31, 43), dtype=np.float32)
+    taps = O.gaussian_taps(9, 2.0)
+    tmp, r = np.zeros_like(img), np.zeros_like(img)
+    assert R.ref_conv_f32(img, 43, 31, np.ascontiguousarray(taps[None, :]), 9, 1, b, 0, 0, tmp) == 0
+    assert R.ref_conv_f32(tmp, 43, 31, np.ascontiguousarray(taps[:, None]), 1, 9, b, 0, 0, r) == 0
+    assert np.array_equal(O.separable(img, taps, taps, boundary=b, contract=0), r)
     # u8 images through the samples' own uchar kernels (blur with + 0.5f, erode / dilate)
     for (mh, mw) in [(3, 3), (5, 5), (7, 7)]:
         img = rng.integers(0, 256, (29, 37), dtype=np.uint8)
