@@ -244,6 +244,10 @@ class PyramidPlan:
     def decompose(self, mode=0, stream=None):
         L.call("hgb_pyramid_decompose", self._h, mode, _stream(stream))
 
+    def wait_test(self, max_polls=0, kind=0, level=0):
+        """Bounded-wait test mode of the plan's launches (hgb_pyramid_plan_wait_test)."""
+        L.call("hgb_pyramid_plan_wait_test", self._h, int(max_polls), int(kind), int(level))
+
     def collapse(self, stream=None):
         L.call("hgb_pyramid_collapse", self._h, _stream(stream))
 

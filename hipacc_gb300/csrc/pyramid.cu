@@ -79,7 +79,11 @@ struct PyrParams {
   unsigned int *done;       // [img * levels + l]: finished tiles of level l
   const int *ntiles_il;     // [img * levels + l]: tiles of level l
   unsigned int *work;       // claim counter (persistent form)
+  unsigned int *abort;      // set when a tile failed: dependants stop waiting (persistent form)
   int *status;
+  long long max_polls;      // limit of every bounded wait
+  int inject_kind;          // wait test (hgb_pyramid_plan_wait_test): 0 none, 1 withhold, 2 no copy
+  int inject_level;
   float mask[25];
   int bmode;
 };
@@ -177,7 +181,10 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
     // patch wrote `stage` with generic stores: order both before the copy
     if (coherent) asm volatile("fence.proxy.async;" ::: "memory");
     mbar_expect_tx(bar, PY_BW * PY_BH * 4);
-    tma_load_3d(stage, &p.maps[t.img * p.levels + t.level], t.bx, t.by, 0, bar);
+    // wait test kind 2: the bytes are expected but no copy is issued, so the
+    // barrier's phase never completes (nothing is in flight when the wait expires)
+    if (!(p.inject_kind == 2 && t.level == p.inject_level))
+      tma_load_3d(stage, &p.maps[t.img * p.levels + t.level], t.bx, t.by, 0, bar);
   }
   const LevelMeta A = p.meta[t.img * p.levels + t.level];
   const LevelMeta B = p.meta[t.img * p.levels + t.level + 1];
@@ -210,12 +217,12 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
       ncy[r] = nn(Sy, gy0 + r, hl) - 2 - ry0;
     }
   }
-  const bool landed = cta_wait(bar, phase);
+  const bool landed = cta_wait(bar, phase, p.max_polls);
   phase ^= 1u;
   if (!landed) {
     if (threadIdx.x == 0) {
       record_status(p.status, HGB_ERR_TIMEOUT);
-      mbar_wait(bar, phase ^ 1u);  // the copy may still land: wait once more (bounded)
+      mbar_wait(bar, phase ^ 1u, p.max_polls);  // the copy may still land: wait once more (bounded)
     }
     return false;
   }
@@ -363,26 +370,41 @@ __global__ void __launch_bounds__(PY_THREADS, 10) pyr_persistent_kernel(const __
       if (t < p.ntiles) {
         const PyrTile tl = p.tiles[t];
         if (tl.level > 0) {
-          // wait (bounded) until the image's previous level is complete
+          // wait (bounded) until the image's previous level is complete; a
+          // failed tile anywhere in the launch ends every wait at once
           const int k = tl.img * p.levels + tl.level - 1;
           const unsigned int need = (unsigned int)p.ntiles_il[k];
           long long spins = 0;
           while (ld_acquire_u32(&p.done[k]) < need) {
-            if (++spins > kMaxSpins) {
+            if (ld_acquire_u32(p.abort)) {
+              s_ok = 0;
+              break;
+            }
+            if (++spins > p.max_polls) {
               s_ok = 0;
               record_status(p.status, HGB_ERR_TIMEOUT);
+              atomicExch(p.abort, 1u);
               break;
             }
             __nanosleep(64);
           }
         }
+        // wait test kind 1: the tile is claimed but never published
+        if (s_ok == 1 && tl.level == p.inject_level && p.inject_kind == 1) s_ok = 2;
       }
     }
     __syncthreads();
     const int t = s_t;
-    if (t >= p.ntiles) return;
+    if (t >= p.ntiles || s_ok == 0) return;
     const PyrTile tl = p.tiles[t];
-    if (s_ok && !pyr_tile(p, tl, stage, gt, cols, rows, ncx, ncy, &bar, phase, true)) return;
+    if (s_ok == 2) {  // uniform: every thread read s_ok after the barrier
+      __syncthreads();  // s_t / s_ok are read before thread 0 claims again
+      continue;
+    }
+    if (!pyr_tile(p, tl, stage, gt, cols, rows, ncx, ncy, &bar, phase, true)) {
+      if (threadIdx.x == 0) atomicExch(p.abort, 1u);
+      return;
+    }
     __syncthreads();
     if (threadIdx.x == 0) red_release_add(&p.done[tl.img * p.levels + tl.level], 1u);
   }
@@ -453,9 +475,11 @@ struct hgb_pyramid_plan {
   CUtensorMap *d_maps = nullptr;   // G_l tensor maps, [img * levels + l]
   PyrTile *d_tiles = nullptr;
   int *d_ntiles = nullptr;
-  unsigned int *d_ctrl = nullptr;  // done counters [n*levels] + claim counter
+  unsigned int *d_ctrl = nullptr;  // done counters [n*levels] + claim counter + abort flag
   int ntiles = 0;
   int persistent_ctas = 0;
+  long long max_polls = kMaxSpins;
+  int inject_kind = 0, inject_level = 0;
 };
 
 extern "C" {
@@ -525,7 +549,7 @@ int hgb_pyramid_plan_create(int n_images, const int *widths, const int *heights,
   if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_meta, P->meta.size() * sizeof(LevelMeta));
   if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_tiles, tiles.size() * sizeof(PyrTile));
   if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_ntiles, nil.size() * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_ctrl, (nil.size() + 1) * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_ctrl, (nil.size() + 2) * sizeof(unsigned int));
   if (e != cudaSuccess) {
     hgb_pyramid_plan_destroy(P);
     return cuda_error(e, "hgb_pyramid_plan_create: allocation");
@@ -613,7 +637,11 @@ static void fill_params(const hgb_pyramid_plan *P, PyrParams *p) {
   p->done = P->d_ctrl;
   p->ntiles_il = P->d_ntiles;
   p->work = P->d_ctrl + (size_t)P->n * P->levels;
+  p->abort = p->work + 1;
   p->status = device_status_word();
+  p->max_polls = P->max_polls;
+  p->inject_kind = P->inject_kind;
+  p->inject_level = P->inject_level;
   memcpy(p->mask, P->mask, sizeof(p->mask));
   p->bmode = P->bmode;
 }
@@ -625,7 +653,7 @@ int hgb_pyramid_decompose(hgb_pyramid_plan *P, int mode, void *stream) {
   PyrParams p;
   fill_params(P, &p);
   if (mode == 0) {
-    HGB_CHECK_CUDA(cudaMemsetAsync(P->d_ctrl, 0, ((size_t)P->n * P->levels + 1) * sizeof(unsigned int), st));
+    HGB_CHECK_CUDA(cudaMemsetAsync(P->d_ctrl, 0, ((size_t)P->n * P->levels + 2) * sizeof(unsigned int), st));
     const int grid = std::min(P->persistent_ctas, P->ntiles);
     cudaEvent_t ev = before_launch(st);
     pyr_persistent_kernel<<<grid, PY_THREADS, 0, st>>>(p);
@@ -659,6 +687,17 @@ int hgb_pyramid_decompose(hgb_pyramid_plan *P, int mode, void *stream) {
       if (rc) return rc;
     }
   }
+  return HGB_OK;
+}
+
+int hgb_pyramid_plan_wait_test(hgb_pyramid_plan *P, long long max_polls, int kind, int level) {
+  HGB_REQUIRE(P, "hgb_pyramid_plan_wait_test: null plan");
+  HGB_REQUIRE(max_polls >= 0, "hgb_pyramid_plan_wait_test: negative poll limit");
+  HGB_REQUIRE(kind >= 0 && kind <= 2, "hgb_pyramid_plan_wait_test: kind must be 0, 1 or 2");
+  HGB_REQUIRE(level >= 0 && level + 1 < P->levels, "hgb_pyramid_plan_wait_test: level has no tiles");
+  P->max_polls = max_polls > 0 ? max_polls : kMaxSpins;
+  P->inject_kind = kind;
+  P->inject_level = level;
   return HGB_OK;
 }
 

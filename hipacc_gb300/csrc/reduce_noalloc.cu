@@ -4,11 +4,10 @@
 // hgb_reduce keeps its scratch (per-block partials, the last-block ticket, the
 // integer accumulator, a result slot) in a per-device workspace that the
 // library grows with cudaMalloc on first use.  Some callers cannot allow that:
-// code that runs while a stream is being captured into a CUDA graph (where
-// cudaMalloc is not permitted), real-time loops that must never block in the
-// allocator, and hosts whose device memory is owned by another allocator with
-// a fixed budget.  This variant uses a fixed array in the library's own device
-// memory instead and calls no allocating routine.
+// real-time frame loops that must never block in the CUDA allocator, and
+// plug-ins inside a host program whose device memory is owned by the host's
+// own allocator with a fixed budget.  This variant uses a fixed array in the
+// library's own device memory instead and calls no allocating routine.
 //
 // Scratch: g_noalloc_scratch, a file-scope __device__ array of
 // kNoAllocBytes (16 KiB of partials for up to kNoAllocMaxBlocks = 1024 blocks

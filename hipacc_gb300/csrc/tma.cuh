@@ -57,9 +57,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
   return ok != 0;
 }
 
-// bounded wait; returns false on timeout (the caller votes and leaves)
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
-  for (long long i = 0; i < kMaxSpins; ++i)
+// bounded wait (at most `limit` polls); returns false on timeout (the caller
+// votes and leaves)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, long long limit = kMaxSpins) {
+  for (long long i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -69,9 +70,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
 // the other threads sleep at the CTA barrier instead of polling the mbarrier
 // (polling warps take issue slots from the CTAs that have work).  Same result
 // on every thread: false when the wait expired.
-__device__ __forceinline__ bool cta_wait(uint64_t *bar, unsigned parity) {
+__device__ __forceinline__ bool cta_wait(uint64_t *bar, unsigned parity, long long limit = kMaxSpins) {
   int late = 0;
-  if (threadIdx.x == 0) late = !mbar_wait(bar, parity);
+  if (threadIdx.x == 0) late = !mbar_wait(bar, parity, limit);
   return !__syncthreads_or(late);
 }
 

@@ -263,9 +263,10 @@ HGB_API int hgb_reduce(const hgb_view *in, const hgb_window *win, int op, void *
 
 /* hgb_reduce for callers that cannot allocate device memory (no counterpart
  * in the reference).  hgb_reduce grows a library workspace with cudaMalloc on
- * first use; code that runs during stream capture, real-time loops that must
- * not block in the allocator, or hosts whose device memory belongs to another
- * allocator cannot allow that.  This entry point allocates nothing: its
+ * first use.  Some callers cannot allow that: real-time frame loops that must
+ * never block in the CUDA allocator, and plug-ins inside a host program whose
+ * device memory belongs to the host's own allocator with a fixed budget.
+ * This entry point allocates nothing: its
  * scratch is a fixed 16.25 KiB array in the library's device memory (block
  * partials for at most 1024 blocks; larger launches return HGB_ERR_LIMIT),
  * held by every GPU that loads the library until exit.  The first call on a
@@ -313,6 +314,17 @@ HGB_API int hgb_pyramid_decompose(hgb_pyramid_plan *plan, int mode, void *stream
 /* Collapse (Restore): G_l = LF(G_{l+1}) + L_l from the bottom level up,
  * into the plan's Gaussian levels. */
 HGB_API int hgb_pyramid_collapse(hgb_pyramid_plan *plan, void *stream);
+/* Test support for the plan's bounded device-side waits (no counterpart in
+ * the reference, whose kernels do not wait on one another).  `max_polls`
+ * limits every wait of the plan's later launches (0 = the default, 2^22
+ * polls).  kind 0: normal operation.  kind 1 (persistent form): the tiles of
+ * `level` are claimed but never published, so the waits of level + 1 on them
+ * run out.  kind 2: the tiles of `level` expect their staged box but no copy
+ * is issued, so their barrier waits run out with nothing in flight.  Either
+ * way the launch ends by itself, the device status word reads
+ * HGB_ERR_TIMEOUT (hgb_device_status) and the context stays usable; nothing
+ * faults or traps. */
+HGB_API int hgb_pyramid_plan_wait_test(hgb_pyramid_plan *plan, long long max_polls, int kind, int level);
 
 /* ------------------------------------------------------------------ */
 /* adjoints                                                            */

@@ -448,24 +448,21 @@ class SobelMagnitude : public Kernel<uchar> {
     check(hgb_sobel_mag(&iv, &ov, mx_.coefficients(), my_.coefficients(), mx_.size_x(), (int)in_.mode(),
                         (int)in_.constant(), sum, mx, current_stream()),
           "SobelMagnitude::execute");
-    fetched_ = false;
   }
-  // read the two scalars back (synchronises the current stream)
+  // read the two scalars back (synchronises the current stream); read on
+  // every call, since a replayed graph rewrites them without a launch() here
   void fetch() {
     execute();
-    if (fetched_) return;
     unsigned long long tmp[2] = {0, 0};
     check(hgb_image_read(scratch_.get(), tmp, current_stream()), "SobelMagnitude::reduced_data");
     host_[0] = tmp[0];
     host_[1] = tmp[1] & 0xffffffffull;
-    fetched_ = true;
   }
   uchar reduce_output() override {
     fetch();
     return (uchar)host_[1];
   }
   std::shared_ptr<hgb_image> scratch_;
-  bool fetched_ = false;
   Accessor<uchar> &in_;
   Mask<int> &mx_, &my_;
   unsigned long long host_[2] = {0, 0};

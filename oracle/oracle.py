@@ -32,11 +32,22 @@ i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 
 
+def reference_tree() -> str:
+    """Location of the Hipacc source tree as the oracle's Makefile resolves it
+    (HIPACC_REF when set); "" when make is unavailable."""
+    try:
+        r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True, check=True)
+    except (OSError, subprocess.CalledProcessError):
+        return ""
+    return r.stdout.strip()
+
+
 def build(force: bool = False) -> None:
     """Compile the restated oracle (and the reference pin when the reference tree exists)."""
     if force or not os.path.exists(LIB_PATH):
         subprocess.run(["make", "-s", "-C", HERE, "liboracle"], check=True)
-    if os.path.isdir("/root/reference/dsl") and (force or not os.path.exists(REF_PATH)):
+    tree = reference_tree()
+    if tree and os.path.isdir(os.path.join(tree, "dsl")) and (force or not os.path.exists(REF_PATH)):
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 

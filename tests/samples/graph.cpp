@@ -2,8 +2,12 @@
 // (samples-public/common/config/cuda-graph.conf): a Gaussian blur, a Sobel
 // magnitude with its fused sum / max, and an RGBA->gray conversion recorded
 // once into a CudaGraph -- the gray conversion on a second stream as an
-// independent branch (fork / join) -- and replayed; the replayed results must
-// equal the eagerly executed ones bit for bit.
+// independent branch (fork / join) -- and replayed.  The replayed results are
+// checked against plain CPU loops of the three kernels (the blur's taps
+// row-major as fused multiply-adds, the Sobel samples' integer arithmetic, the
+// integer gray weights) and against the eager execution; then new inputs are
+// written and the same graph replayed again, so that a replay that re-used
+// stale results would fail.
 #include <hipacc_gb300/hipacc.hpp>
 
 #include "common.hpp"
@@ -57,18 +61,61 @@ int main() {
   for (int i = 0; i < 10; ++i) graph.launch();
   graph.synchronize();
 
-  const float *a = fout_e.data(), *b = fout_g.data();
-  for (int p = 0; p < width * height; ++p) REQUIRE(a[p] == b[p]);
-  const uchar *m1 = mag_e.data(), *m2 = mag_g.data();
-  unsigned long long s = 0;
-  for (int p = 0; p < width * height; ++p) {
-    REQUIRE(m1[p] == m2[p]);
-    s += m2[p];
-  }
-  REQUIRE(sob_g.reduced_sum() == s && sob_g.reduced_sum() == sob_e.reduced_sum());
-  REQUIRE(sob_g.reduced_max() == sob_e.reduced_max());
-  const uchar *g1 = gray_e.data(), *g2 = gray_g.data();
-  for (int p = 0; p < width * height; ++p) REQUIRE(g1[p] == g2[p]);
+  // CPU loops of the three kernels on the current host inputs
+  auto check_all = [&](const std::vector<float> &fi, const std::vector<unsigned char> &ui,
+                       const std::vector<unsigned char> &ci, bool with_eager) {
+    const float *b = fout_g.data();
+    const float *a = with_eager ? fout_e.data() : nullptr;
+    for (int y = 0; y < height; ++y)
+      for (int x = 0; x < width; ++x) {
+        float acc = 0.0f;
+        for (int j = -1; j <= 1; ++j)
+          for (int i = -1; i <= 1; ++i)
+            acc = std::fmaf(coef[j + 1][i + 1], fi[(size_t)mirror(y + j, height) * width + mirror(x + i, width)], acc);
+        REQUIRE(b[(size_t)y * width + x] == acc);
+        if (a) REQUIRE(a[(size_t)y * width + x] == acc);
+      }
+    const uchar *m2 = mag_g.data();
+    const uchar *m1 = with_eager ? mag_e.data() : nullptr;
+    unsigned long long s = 0;
+    unsigned mx_ = 0;
+    for (int y = 0; y < height; ++y)
+      for (int x = 0; x < width; ++x) {
+        int gx = 0, gy = 0;
+        for (int j = -1; j <= 1; ++j)
+          for (int i = -1; i <= 1; ++i) {
+            const int v = ui[(size_t)clampi(y + j, 0, height - 1) * width + clampi(x + i, 0, width - 1)];
+            gx += sx[j + 1][i + 1] * v;
+            gy += sy[j + 1][i + 1] * v;
+          }
+        const int m = std::min(std::abs(gx) + std::abs(gy), 255);
+        REQUIRE(m2[(size_t)y * width + x] == m);
+        if (m1) REQUIRE(m1[(size_t)y * width + x] == m);
+        s += (unsigned)m;
+        mx_ = std::max<unsigned>(mx_, (unsigned)m);
+      }
+    REQUIRE(sob_g.reduced_sum() == s && sob_g.reduced_max() == mx_);
+    if (with_eager) REQUIRE(sob_e.reduced_sum() == s && sob_e.reduced_max() == mx_);
+    const uchar *g2 = gray_g.data();
+    const uchar *g1 = with_eager ? gray_e.data() : nullptr;
+    for (int p = 0; p < width * height; ++p) {
+      const int g = (77 * ci[4 * p] + 150 * ci[4 * p + 1] + 29 * ci[4 * p + 2]) >> 8;
+      REQUIRE(g2[p] == g);
+      if (g1) REQUIRE(g1[p] == g);
+    }
+  };
+  check_all(f, u, rgba, true);
+
+  // new inputs into the same device images, the same graph replayed
+  f = random_floats(width * height, 31);
+  u = random_bytes(width * height, 32);
+  rgba = random_bytes(width * height * 4, 33);
+  fin = f.data();
+  uin = u.data();
+  cin = reinterpret_cast<const uchar4 *>(rgba.data());
+  graph.launch();
+  graph.synchronize();
+  check_all(f, u, rgba, false);
   std::printf("Test PASSED\n");
   return 0;
 }

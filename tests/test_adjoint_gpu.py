@@ -118,3 +118,46 @@ def test_adjoint_2048(gpu, oracle):
     L0, dx0, dm0, ds0 = _oracle_batch(oracle, x, t, mask, sm, 0.15, 3)
     assert abs(L - L0) <= LOSS_TOL * abs(L0)
     assert rel(dx, dx0) <= ADJ_TOL and rel(dm, dm0) <= ADJ_TOL and abs(ds - ds0) <= ADJ_TOL * abs(ds0)
+
+
+@pytest.mark.parametrize("boundary", [1, 3])
+def test_adjoint_full_batch_16x2048(gpu, oracle, boundary):
+    """The differentiation workload as it is benchmarked: a batch of 16
+    2048x2048 images in the fused mode.  The batch loss is the mean over every
+    pixel of every image, so image b's input gradient is its single-image
+    gradient divided by 16: images 0 and 15 of the batch are checked against
+    the FP64 oracle that way.  The batch's loss, mask and sigma gradients must
+    be the mean of the 16 single-image results (each a separate launch), and
+    the single-image results of images 0 and 15 match the FP64 oracle."""
+    B, H, W = 16, 2048, 2048
+    rng = np.random.default_rng(60 + boundary)
+    x = torch.rand((B, H, W), device="cuda", generator=torch.Generator("cuda").manual_seed(61 + boundary))
+    t = torch.empty_like(x)
+    gpu.local_op(x, t, mask=oracle.gaussian_mask(7, 1.5), boundary=boundary)
+    mask = rng.normal(0, 0.02, (7, 7)).astype(np.float32)
+    mask[3, 3] += 0.8
+    sm = oracle.spatial_mask(9, 2.0)
+    sigma = 0.15
+    md = torch.from_numpy(mask).cuda()
+    sd = torch.tensor([sigma], dtype=torch.float32, device="cuda")
+    loss, gx, gm, gs = gpu.conv_bilateral_mse(x, t, md, sd, sm, boundary, 0)
+    torch.cuda.synchronize()
+    Lb, dmb, dsb = float(loss.item()), gm.cpu().numpy().astype(np.float64), float(gs.item())
+    # the 16 single-image launches
+    singles = []
+    for b in range(B):
+        l1, g1, m1, s1 = gpu.conv_bilateral_mse(x[b:b + 1], t[b:b + 1], md, sd, sm, boundary, 0)
+        singles.append((float(l1.item()), g1, m1.cpu().numpy().astype(np.float64), float(s1.item())))
+    torch.cuda.synchronize()
+    assert abs(Lb - np.mean([s[0] for s in singles])) <= 1e-6 * abs(Lb)
+    assert rel(dmb, np.mean([s[2] for s in singles], axis=0)) <= 1e-5
+    assert abs(dsb - np.mean([s[3] for s in singles])) <= 1e-5 * abs(dsb)
+    for b in (0, B - 1):
+        # the batch's gradient of image b is its single-image gradient / 16
+        assert rel(gx[b].cpu().numpy(), singles[b][1][0].cpu().numpy() / B) <= 1e-6
+        xb, tb = x[b].cpu().numpy(), t[b].cpu().numpy()
+        l0, dx0, dm0, ds0 = oracle.c5_grad(xb, tb, mask.astype(np.float64), sm.astype(np.float64), sigma, boundary)
+        assert abs(singles[b][0] - l0) <= LOSS_TOL * abs(l0), (b, singles[b][0], l0)
+        assert rel(gx[b].cpu().numpy(), dx0 / B) <= ADJ_TOL, (b, rel(gx[b].cpu().numpy(), dx0 / B))
+        assert rel(singles[b][2], dm0) <= ADJ_TOL, (b, rel(singles[b][2], dm0))
+        assert abs(singles[b][3] - ds0) <= ADJ_TOL * abs(ds0), (b, singles[b][3], ds0)

@@ -7,6 +7,8 @@ bit (blur taps row-major with fused multiply-add; nearest-neighbour and linear
 filtering mappings in FP32 with the contracted mapping), and the collapse must
 restore the input (Restore, samples-public/5_Other/Gaussian_Laplacian_Pyramid).
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 import torch
@@ -85,3 +87,92 @@ def test_pyramid_status_clean(gpu):
     st = C.c_int(-1)
     L.call("hgb_device_status", C.byref(st))
     assert st.value == 0
+
+
+def test_pyramid_full_batch_all_modes(gpu, oracle):
+    """The batching workload exactly as it is benchmarked: 64 FP32 images with
+    w, h uniform in [257, 4096] (seed 4096), 8 levels, MIRROR.  Level 7 comes
+    down to 2-3 pixels on some images (the repeated MIRROR reflection), and the
+    persistent launch walks a work-list of every tile of every level.  Every
+    G_l and L_l of every image must equal the oracle's in all three launch
+    forms; outputs are poisoned with NaN first, so a tile that was never
+    written fails."""
+    from hipacc_gb300 import _lib as L
+
+    rng = np.random.default_rng(4096)
+    ws = rng.integers(257, 4097, 64)
+    hs = rng.integers(257, 4097, 64)
+    levels = 8
+    assert min(int(ws.min()), int(hs.min())) >> (levels - 1) <= 3  # the tiny-level regime is exercised
+    mask = oracle.binomial5()
+    plans = [gpu.PyramidPlan(ws, hs, levels, mask, oracle.MIRROR) for _ in range(3)]
+    imgs = []
+    prng = np.random.default_rng(77)
+    for i in range(64):
+        im = prng.random((int(hs[i]), int(ws[i])), dtype=np.float32)
+        imgs.append(im)
+        d = torch.from_numpy(im).cuda()
+        for p in plans:
+            p.gauss(i, 0).copy_(d)
+            for l in range(1, levels):
+                p.gauss(i, l).fill_(float("nan"))
+            for l in range(levels - 1):
+                p.lap(i, l).fill_(float("nan"))
+    for mode, p in enumerate(plans):
+        p.decompose(mode)
+    torch.cuda.synchronize()
+    st = C.c_int(-1)
+    L.call("hgb_device_status", C.byref(st))
+    assert st.value == 0
+    for i, im in enumerate(imgs):
+        g, lap = oracle.pyramid_decompose(im, levels, mask, oracle.MIRROR, contract=1)
+        gd = [torch.from_numpy(a).cuda() for a in g]
+        ld = [torch.from_numpy(a).cuda() for a in lap]
+        for mode, p in enumerate(plans):
+            for l in range(levels):
+                assert torch.equal(p.gauss(i, l), gd[l]), (mode, i, l)
+                if l + 1 < levels:
+                    assert torch.equal(p.lap(i, l), ld[l]), (mode, i, l)
+    for p in plans:
+        p.close()
+
+
+@pytest.mark.parametrize("kind,level,mode", [(1, 0, 0), (1, 2, 0), (2, 1, 0), (2, 0, 1)])
+def test_pyramid_bounded_waits_expire(gpu, oracle, kind, level, mode):
+    """A wait that can never be satisfied runs out after a short poll limit:
+    kind 1 withholds the completion of a level's tiles (the next level's
+    inter-level waits run out), kind 2 issues no copy for a level's staged
+    boxes (their barrier waits run out).  The launch ends by itself with
+    HGB_ERR_TIMEOUT in the device status word, and the same plan then decomposes
+    correctly once the test mode is off."""
+    from hipacc_gb300 import _lib as L
+
+    levels = 5
+    plan, imgs = _plan(gpu, oracle, SIZES[:4], levels, oracle.MIRROR, 9)
+    plan.wait_test(max_polls=2000, kind=kind, level=level)
+    plan.decompose(mode)
+    st = C.c_int(-1)
+    L.call("hgb_device_status", C.byref(st))  # synchronises, reads and clears the word
+    assert st.value == L.ERR_TIMEOUT
+    plan.wait_test(0, 0, 0)
+    plan.decompose(mode)
+    L.call("hgb_device_status", C.byref(st))
+    assert st.value == 0
+    for i, im in enumerate(imgs):
+        g, lap = oracle.pyramid_decompose(im, levels, oracle.binomial5(), oracle.MIRROR, contract=1)
+        for l in range(levels - 1):
+            assert np.array_equal(plan.lap(i, l).cpu().numpy(), lap[l]), (i, l)
+            assert np.array_equal(plan.gauss(i, l + 1).cpu().numpy(), g[l + 1]), (i, l)
+    plan.close()
+
+
+def test_pyramid_wait_test_arguments(gpu, oracle):
+    from hipacc_gb300 import _lib as L
+
+    plan, _ = _plan(gpu, oracle, SIZES[:1], 3, oracle.MIRROR, 1)
+    lib = L.load()
+    assert lib.hgb_pyramid_plan_wait_test(plan._h, -1, 0, 0) == L.ERR_INVALID
+    assert lib.hgb_pyramid_plan_wait_test(plan._h, 10, 3, 0) == L.ERR_INVALID
+    assert lib.hgb_pyramid_plan_wait_test(plan._h, 10, 1, 2) == L.ERR_INVALID  # the last level has no tiles
+    assert lib.hgb_pyramid_plan_wait_test(None, 10, 1, 0) == L.ERR_INVALID
+    plan.close()

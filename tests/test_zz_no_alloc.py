@@ -1,8 +1,9 @@
 """GPU: hgb_reduce_noalloc, the reduction entry point that allocates nothing.
 
-Callers that cannot allocate device memory (stream capture, allocator-free
-real-time loops, hosts with their own device allocator) use it instead of
-hgb_reduce, which grows a library workspace with cudaMalloc.  Its scratch is a
+Callers that cannot allocate device memory (real-time frame loops that must
+never block in the CUDA allocator, plug-ins whose host program owns the device
+memory through its own allocator) use it instead of hgb_reduce, which grows a
+library workspace with cudaMalloc.  Its scratch is a
 fixed array in the library's device memory.  Checked here through the C ABI
 against hgb_reduce on the same inputs, on two calls in a row (the second call
 reuses the array the first one left behind), and the device's free memory is
