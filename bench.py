@@ -46,6 +46,7 @@ NSETS = 16
 # this workload (profiles/ holds the summary and the command); most of each
 # kernel's output is still in L2 when the capture ends, so writes read low
 NCU_TRAFFIC = {"sobel3_tma_kernel": 16845056 + 0, "gray_bulk_kernel": 67121664 + 1593088}
+E2E_STEPS = 64  # end-to-end steps timed, independent of --steps
 METRIC = "Gpixels/s (Sobel3x3 MIRROR + u64 sum + u8 max, and RGBA->gray, 4096x4096)"
 
 
@@ -409,7 +410,7 @@ def gauss_taps(k, sigma):
     return (g / g.sum()).astype(np.float32)
 
 
-OTHER_SECTIONS = ("gaussian", "precision", "pyramid", "diff", "histogram")
+OTHER_SECTIONS = ("integer", "gaussian", "precision", "pyramid", "diff", "histogram")
 
 
 def measure_other_configs(dev, peak_gbs, only=None):
@@ -426,6 +427,8 @@ def measure_other_configs(dev, peak_gbs, only=None):
     def want(sec):
         return only is None or only == sec
 
+    if only == "integer":  # the headline step's two kernels alone, few launches (for a profiler)
+        _integer(dev, peak_gbs, s, res)
     if want("gaussian"):
         _gaussian(dev, peak_gbs, s, res, q)
     if want("precision"):
@@ -437,6 +440,28 @@ def measure_other_configs(dev, peak_gbs, only=None):
     if want("histogram"):
         _histogram(dev, peak_gbs, s, res, q)
     return res
+
+
+def _integer(dev, peak_gbs, s, res):
+    import torch
+
+    from hipacc_gb300 import api
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    n = 4
+    imgs = [torch.randint(0, 256, (H, W), dtype=torch.uint8, device=dev, generator=g) for _ in range(n)]
+    rgbas = [torch.randint(0, 256, (H, W, 4), dtype=torch.uint8, device=dev, generator=g) for _ in range(n)]
+    mags = [torch.empty_like(x) for x in imgs]
+    grays = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(n)]
+    acc = torch.zeros((n, 2), dtype=torch.int64, device=dev)
+    us = graph_time_us(lambda i: api.sobel_mag(imgs[i], mags[i], boundary=api.MIRROR, sum_out=acc[i, 0:1],
+                                               max_out=acc[i, 1:2], stream=s), n, s, 2)
+    res["sobel3_mirror_sum_max_4096"] = {"us_per_launch": us, "achieved_gbs": SOBEL_BYTES / us / 1e3,
+                                         "frac_hbm": SOBEL_BYTES / us / 1e3 / peak_gbs}
+    us = graph_time_us(lambda i: api.gray(rgbas[i], grays[i], stream=s), n, s, 2)
+    res["rgba_gray_4096"] = {"us_per_launch": us, "achieved_gbs": GRAY_BYTES / us / 1e3,
+                             "frac_hbm": GRAY_BYTES / us / 1e3 / peak_gbs}
 
 
 def _histogram(dev, peak_gbs, s, res, q):
@@ -590,7 +615,7 @@ def run_e2e(args, L, dev, rank):
 
     lib = L.load()
     rng = np.random.default_rng(99 + rank)
-    n_e2e = max(4, min(args.steps // 8, 200))
+    n_e2e = E2E_STEPS
     h_img = torch.from_numpy(rng.integers(0, 256, (H, W), dtype=np.uint8)).pin_memory()
     h_rgba = torch.from_numpy(rng.integers(0, 256, (H, W, 4), dtype=np.uint8)).pin_memory()
     nset = 2
