@@ -310,3 +310,17 @@ def local_op_adjoint(grad_out, mask, boundary=CLAMP, inp=None, want_grad_in=True
            None if vgi is None else C.byref(vgi), m_host, m_dev, mw, mh, boundary,
            None if gm is None else C.c_void_p(gm.data_ptr()), _stream(stream))
     return gi, gm
+
+
+def bilateral_adjoint(inp, grad_out, smask, sigma_r, boundary=CLAMP, const=0.0, want_grad_in=True,
+                      want_grad_sigma=True, stream=None):
+    """Adjoint of the bilateral filter: (grad_in, grad_sigma [1 float]) for grad_out = dL/dy."""
+    gi = torch.empty_like(grad_out) if want_grad_in else None
+    gs = torch.zeros(1, dtype=torch.float32, device=inp.device) if want_grad_sigma else None
+    s = np.ascontiguousarray(smask, np.float32)
+    vi, vg = view(inp), view(grad_out)
+    vgi = view(gi) if gi is not None else None
+    L.call("hgb_bilateral_adjoint", C.byref(vi), C.byref(vg), s.ctypes.data_as(C.c_void_p), s.shape[0],
+           float(sigma_r), boundary, float(const), None if vgi is None else C.byref(vgi),
+           None if gs is None else C.c_void_p(gs.data_ptr()), _stream(stream))
+    return gi, gs

@@ -341,6 +341,23 @@ HGB_API int hgb_local_op_adjoint(const hgb_view *in, const hgb_view *grad_out, c
                          const float *mask_dev, int mask_w, int mask_h, int boundary, float *grad_mask_dev,
                          void *stream);
 
+/* Adjoint of the bilateral filter hgb_bilateral (the body of
+ * samples-public/3_Preprocessing/Bilateral_Filter/src/main.cpp:63-77, FP32
+ * storage): for grad_out = dL/dy it returns
+ *   grad_in (may be NULL)        = dL/din, with the boundary transposed: every
+ *                                  tap that read a pixel through CLAMP / MIRROR /
+ *                                  REPEAT sends its gradient there, CONSTANT taps
+ *                                  carry none;
+ *   grad_sigma_dev (may be NULL) = dL/dsigma_r (one float, summed over the batch,
+ *                                  combined in FP64 in a fixed order).
+ * The range weights are recomputed, never stored.  Same smask / size / sigma_r /
+ * boundary / const_val as the forward; size odd, 3..13.  Uses the library
+ * workspace (8 bytes per pixel): calls sharing it must be ordered on one
+ * stream. */
+HGB_API int hgb_bilateral_adjoint(const hgb_view *in, const hgb_view *grad_out, const float *smask, int size,
+                                  float sigma_r, int boundary, float const_val, const hgb_view *grad_in,
+                                  float *grad_sigma_dev, void *stream);
+
 /* Forward + adjoint of the differentiation workload
  *   y1 = conv(x, mask), y = bilateral(y1; smask, sigma_r), loss = mean((y - t)^2)
  * in two fused kernels (forward with the loss gradient in its epilogue;

@@ -694,4 +694,54 @@ double orc_c5_grad_f64(const double *x, const double *t, int w, int h, const dou
   return L;
 }
 
+// Adjoint of the bilateral filter in FP64, the forward of
+// samples-public/3_Preprocessing/Bilateral_Filter/src/main.cpp:63-77 (the
+// `bilateral` template above, taps through the boundary remap, CONSTANT taps
+// reading cval):  y_p = N_p / W_p,  N_p = sum_o w_po v_q,  W_p = sum_o w_po,
+// w_po = smask_o exp(-c (v_q - in_p)^2),  c = 1 / (2 sigma_r^2),  q = r(p + o).
+// Given g = dL/dy:
+//   a_p = g_p / W_p
+//   dL/din_q += a_p w_po (1 - 2c (v_q - y_p)(v_q - in_p))    (q a pixel, not the constant)
+//   dL/din_p += a_p sum_o w_po (v_q - y_p) 2c (v_q - in_p)
+//   dL/dc     = sum_p a_p sum_o w_po (v_q - y_p) (-(v_q - in_p)^2),  dL/dsigma_r = -dL/dc / sigma_r^3
+// grad_in (w x h, dense) is overwritten; returns dL/dsigma_r.
+double orc_bilateral_adjoint_f64(const double *in, const double *g, int w, int h, const double *smask, int size,
+                                 double sigma_r, int bmode, double cval, double *grad_in) {
+  const int r = size / 2;
+  const double c = 0.5 / (sigma_r * sigma_r);
+  const long n = (long)w * h;
+  std::fill(grad_in, grad_in + n, 0.0);
+  double dc = 0.0;
+  std::vector<double> vq((size_t)size * size);
+  std::vector<long> iq((size_t)size * size);
+  for (int py = 0; py < h; ++py)
+    for (int px = 0; px < w; ++px) {
+      const long p = (long)py * w + px;
+      const double ctr = in[p];
+      double N = 0.0, W = 0.0;
+      for (int oy = 0; oy < size; ++oy)
+        for (int ox = 0; ox < size; ++ox) {
+          const int k = oy * size + ox;
+          const int qx = remap_idx(bmode, px + ox - r, 0, w), qy = remap_idx(bmode, py + oy - r, 0, h);
+          iq[k] = (qx == kConstIdx || qy == kConstIdx) ? -1 : (long)qy * w + qx;
+          vq[k] = iq[k] < 0 ? cval : in[iq[k]];
+          const double d = vq[k] - ctr;
+          const double wt = smask[k] * std::exp(-c * d * d);
+          N += wt * vq[k];
+          W += wt;
+        }
+      const double y = N / W, a = g[p] / W;
+      double ctr_acc = 0.0;
+      for (int k = 0; k < size * size; ++k) {
+        const double d = vq[k] - ctr;
+        const double wt = smask[k] * std::exp(-c * d * d);
+        if (iq[k] >= 0) grad_in[iq[k]] += a * wt * (1.0 - 2.0 * c * (vq[k] - y) * d);
+        ctr_acc += wt * (vq[k] - y) * 2.0 * c * d;
+        dc += a * wt * (vq[k] - y) * (-d * d);
+      }
+      grad_in[p] += a * ctr_acc;
+    }
+  return dc * (-1.0 / (sigma_r * sigma_r * sigma_r));
+}
+
 }  // extern "C"

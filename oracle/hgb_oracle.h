@@ -120,6 +120,10 @@ void orc_pyramid_collapse_f32(float **out, float **lap, int w, int h, int levels
  * finite differences); `orc_c5_grad_f64` adds the hand adjoint. */
 double orc_c5_loss_f64(const double *x, const double *t, int w, int h, const double *mask, int mk,
                        const double *smask, int sk, double sigma_r, int bmode, int nthreads);
+/* Adjoint of the bilateral filter (FP64): dL/din into grad_in (dense w x h) for
+ * dL/dy = g; returns dL/dsigma_r. */
+double orc_bilateral_adjoint_f64(const double *in, const double *g, int w, int h, const double *smask, int size,
+                                 double sigma_r, int bmode, double cval, double *grad_in);
 double orc_c5_grad_f64(const double *x, const double *t, int w, int h, const double *mask, int mk,
                        const double *smask, int sk, double sigma_r, int bmode, double *dx,
                        double *dmask, double *dsigma, int nthreads);

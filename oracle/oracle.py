@@ -102,6 +102,9 @@ def lib():
         L.orc_c5_grad_f64.argtypes = [f64p, f64p, C.c_int, C.c_int, f64p, C.c_int, f64p, C.c_int, C.c_double,
                                       C.c_int, f64p, f64p, f64p, C.c_int]
         L.orc_c5_grad_f64.restype = C.c_double
+        L.orc_bilateral_adjoint_f64.argtypes = [f64p, f64p, C.c_int, C.c_int, f64p, C.c_int, C.c_double, C.c_int,
+                                                C.c_double, f64p]
+        L.orc_bilateral_adjoint_f64.restype = C.c_double
         _lib = L
     return _lib
 
@@ -358,6 +361,17 @@ def c5_grad(x, t, mask, smask, sigma_r, boundary=CLAMP, nthreads=0):
                                  np.ascontiguousarray(smask, np.float64), smask.shape[0], sigma_r, boundary, dx,
                                  dmask, dsig, nt)
     return float(loss), dx, dmask, float(dsig[0])
+
+
+def bilateral_adjoint(img, grad_out, smask, sigma_r, boundary=CLAMP, const=0.0):
+    """FP64 adjoint of the bilateral filter: (dL/din, dL/dsigma_r) for dL/dy = grad_out."""
+    x = np.ascontiguousarray(img, np.float64)
+    g = np.ascontiguousarray(grad_out, np.float64)
+    h, w = x.shape
+    gi = np.zeros_like(x)
+    ds = lib().orc_bilateral_adjoint_f64(x, g, w, h, np.ascontiguousarray(smask, np.float64), smask.shape[0],
+                                         float(sigma_r), boundary, float(const), gi)
+    return gi, float(ds)
 
 
 # ---- standard masks (FP64 construction rounded once to FP32) ----
