@@ -410,7 +410,7 @@ def gauss_taps(k, sigma):
     return (g / g.sum()).astype(np.float32)
 
 
-OTHER_SECTIONS = ("integer", "gaussian", "precision", "pyramid", "diff", "histogram")
+OTHER_SECTIONS = ("integer", "gaussian", "precision", "pyramid", "diff", "histogram", "pipelines")
 
 
 def measure_other_configs(dev, peak_gbs, only=None):
@@ -439,6 +439,8 @@ def measure_other_configs(dev, peak_gbs, only=None):
         _diff(dev, s, res, q)
     if want("histogram"):
         _histogram(dev, peak_gbs, s, res, q)
+    if want("pipelines"):
+        _pipelines(dev, peak_gbs, s, res, q)
     return res
 
 
@@ -462,6 +464,36 @@ def _integer(dev, peak_gbs, s, res):
     us = graph_time_us(lambda i: api.gray(rgbas[i], grays[i], stream=s), n, s, 2)
     res["rgba_gray_4096"] = {"us_per_launch": us, "achieved_gbs": GRAY_BYTES / us / 1e3,
                              "frac_hbm": GRAY_BYTES / us / 1e3 / peak_gbs}
+
+
+def _pipelines(dev, peak_gbs, s, res, q):
+    import torch
+
+    from hipacc_gb300 import api
+
+    # the Harris corner and Unsharp sample programs at the samples' 4032 x 3024,
+    # fused against the reference's nine / five launches; 8 rotating images
+    # (Harris 195 MB, Unsharp 780 MB of inputs and outputs, larger than L2)
+    w, h, n = 4032, 3024, 8
+    g = torch.Generator(device=dev)
+    g.manual_seed(13)
+    px = w * h
+    ins = [torch.randint(0, 256, (h, w), dtype=torch.uint8, device=dev, generator=g) for _ in range(n)]
+    outs = [torch.empty_like(x) for x in ins]
+    for mode, name in ((0, "fused_1launch"), (1, "reference_9launches")):
+        us = graph_time_us(lambda i: api.harris(ins[i], outs[i], boundary=api.CLAMP, mode=mode, stream=s), n, s,
+                           1 if q else 10)
+        res[f"harris3_{w}x{h}_{name}"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                          "achieved_gbs": 2 * px / us / 1e3, "frac_hbm": 2 * px / us / 1e3 / peak_gbs}
+    del ins, outs
+    ins = [torch.randint(0, 256, (h, w, 4), dtype=torch.uint8, device=dev, generator=g) for _ in range(n)]
+    outs = [torch.empty_like(x) for x in ins]
+    for mode, name in ((0, "fused_1launch"), (1, "reference_5launches")):
+        us = graph_time_us(lambda i: api.unsharp(ins[i], outs[i], boundary=api.CLAMP, mode=mode, stream=s), n, s,
+                           1 if q else 10)
+        res[f"unsharp3_{w}x{h}_{name}"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                           "achieved_gbs": 8 * px / us / 1e3, "frac_hbm": 8 * px / us / 1e3 / peak_gbs}
+    del ins, outs
 
 
 def _histogram(dev, peak_gbs, s, res, q):

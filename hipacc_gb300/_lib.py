@@ -81,6 +81,8 @@ SIGNATURES = {
     "hgb_point_binary": (i32, [i32, VP, VP, VP, f32, f32, vp]),
     "hgb_convert": (i32, [VP, VP, vp]),
     "hgb_resample": (i32, [VP, VP, i32, vp]),
+    "hgb_harris_corner": (i32, [VP, VP, f32, f32, i32, i32, vp]),
+    "hgb_unsharp": (i32, [VP, VP, i32, i32, vp]),
     "hgb_reduce": (i32, [VP, WP, i32, vp, vp, vp]),
     "hgb_reduce_noalloc": (i32, [VP, WP, i32, vp, vp, vp]),
     "hgb_pyramid_plan_create": (i32, [i32, vp, vp, i32, vp, i32, C.POINTER(vp)]),

@@ -324,3 +324,21 @@ def bilateral_adjoint(inp, grad_out, smask, sigma_r, boundary=CLAMP, const=0.0, 
            float(sigma_r), boundary, float(const), None if vgi is None else C.byref(vgi),
            None if gs is None else C.c_void_p(gs.data_ptr()), _stream(stream))
     return gi, gs
+
+
+def harris(inp, out=None, k=0.04, threshold=20000.0, boundary=CLAMP, mode=0, stream=None):
+    """The Harris corner program (u8 in, 0 / 1 u8 out); mode 0 fused, 1 nine launches."""
+    if out is None:
+        out = torch.empty_like(inp)
+    vi, vo = view(inp), view(out)
+    L.call("hgb_harris_corner", C.byref(vi), C.byref(vo), float(k), float(threshold), boundary, mode, _stream(stream))
+    return out
+
+
+def unsharp(rgba, out=None, boundary=CLAMP, mode=0, stream=None):
+    """The Unsharp program (uchar4 in and out); mode 0 fused, 1 five launches."""
+    if out is None:
+        out = torch.empty_like(rgba)
+    vi, vo = view(rgba, rgba=True), view(out, rgba=True)
+    L.call("hgb_unsharp", C.byref(vi), C.byref(vo), boundary, mode, _stream(stream))
+    return out

@@ -243,6 +243,32 @@ HGB_API int hgb_convert(const hgb_view *in, const hgb_view *out, void *stream);
 HGB_API int hgb_resample(const hgb_view *in, const hgb_view *out, int imode, void *stream);
 
 /* ------------------------------------------------------------------ */
+/* multi-kernel programs as fused chains                               */
+/* ------------------------------------------------------------------ */
+
+/* The Harris corner program (samples-public/3_Preprocessing/Harris_Corner/
+ * src/main.cpp:56-166,258-307, 3x3 masks; nine kernels there: two
+ * derivatives over Domains with a /6, three squares, three integer Gaussians
+ * with a /16, the response R = det - k trace^2 against `threshold`).  u8 in,
+ * u8 out (0 or 1 per pixel), every local operator reading through `boundary`
+ * (CONSTANT taps read 0).  mode 0: one fused kernel (the intermediates stay
+ * in shared memory); mode 1: the nine launches with short intermediates in
+ * the library workspace (for comparison).  Bit-exact either way. */
+HGB_API int hgb_harris_corner(const hgb_view *in, const hgb_view *out, float k, float threshold, int boundary,
+                              int mode, void *stream);
+
+/* The Unsharp program (samples-public/1_Local_Operators/Unsharp/src/main.cpp:
+ * 53-149,203-247, 3x3; five kernels there: gamma-corrected luminance, Gaussian
+ * blur through `boundary`, sharpen, ratio, scale of the RGB channels).
+ * uchar4 in and out (alpha copied).  The luminance's powf terms are the host
+ * C library's (the CPU back end's function) and its double sum is reproduced
+ * exactly, so the result equals the CPU back end's bit for bit; a channel
+ * product outside [0, 256) keeps the low byte of its truncation to an int, as
+ * the CPU back end's conversion does.  mode 0: one fused kernel; mode 1: the
+ * five launches with float intermediates in the library workspace. */
+HGB_API int hgb_unsharp(const hgb_view *in, const hgb_view *out, int boundary, int mode, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* global reductions                                                   */
 /* ------------------------------------------------------------------ */
 

@@ -482,6 +482,43 @@ class ColorConversion : public Kernel<uchar> {
   int wr_, wg_, wb_, sh_;
 };
 
+// The Harris corner program of samples-public/3_Preprocessing/Harris_Corner
+// (3x3; derivatives, squares, Gaussians, response) as one kernel object: the
+// accessor's boundary applies to every local operator of the chain.  mode 0
+// runs it fused, mode 1 as the reference's nine launches.
+class HarrisCorner : public Kernel<uchar> {
+ public:
+  HarrisCorner(IterationSpace<uchar> &it, Accessor<uchar> &in, float k = 0.04f, float threshold = 20000.0f,
+               int mode = 0)
+      : Kernel<uchar>(it), in_(in), k_(k), thr_(threshold), mode_(mode) {}
+
+ protected:
+  void launch() override {
+    hgb_view iv = in_.image().view(), ov = this->out_view();
+    check(hgb_harris_corner(&iv, &ov, k_, thr_, (int)in_.mode(), mode_, current_stream()), "HarrisCorner::execute");
+  }
+  Accessor<uchar> &in_;
+  float k_, thr_;
+  int mode_;
+};
+
+// The Unsharp program of samples-public/1_Local_Operators/Unsharp (3x3;
+// luminance, blur, sharpen, ratio, scale) as one kernel object; the accessor's
+// boundary applies to the blur.  mode 0 fused, mode 1 the reference's five
+// launches.
+class UnsharpMask : public Kernel<uchar4> {
+ public:
+  UnsharpMask(IterationSpace<uchar4> &it, Accessor<uchar4> &in, int mode = 0) : Kernel<uchar4>(it), in_(in), mode_(mode) {}
+
+ protected:
+  void launch() override {
+    hgb_view iv = in_.image().view(), ov = this->out_view();
+    check(hgb_unsharp(&iv, &ov, (int)in_.mode(), mode_, current_stream()), "UnsharpMask::execute");
+  }
+  Accessor<uchar4> &in_;
+  int mode_;
+};
+
 // output() = input(): a plain copy, or a resampling read for NN / LF accessors
 template <typename T>
 class Copy : public Kernel<T> {

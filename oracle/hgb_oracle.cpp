@@ -694,6 +694,112 @@ double orc_c5_grad_f64(const double *x, const double *t, int w, int h, const dou
   return L;
 }
 
+// Harris corner program (samples-public/3_Preprocessing/Harris_Corner/src/main.cpp:56-166,
+// 258-307, SIZE 3): every local operator reads through the boundary remap
+// (CONSTANT taps read 0).
+//   dx = (short)(sum_dom(in * cx) / 6), dy likewise with cy (Domain: zero cells
+//        skipped; short sum, C division truncating toward zero)
+//   sx = dx * dx, sy = dy * dy, sxy = dx * dy (short)
+//   Gx = (short)(sum_mask(sx * m) / 16) over the 3x3 [1 2 1; 2 4 2; 1 2 1] mask
+//        (int sum), Gy, Gxy likewise
+//   R  = (float)(Gx * Gy - Gxy * Gxy) - (k * (float)(Gx + Gy)) * (float)(Gx + Gy),
+//        each float operation rounded separately; out = R > threshold
+void orc_harris_u8(const uint8_t *in, int w, int h, int bmode, float k, float threshold, uint8_t *out,
+                   int nthreads) {
+  static const int cx[9] = {-1, 0, 1, -1, 0, 1, -1, 0, 1};
+  static const int cy[9] = {-1, -1, -1, 0, 0, 0, 1, 1, 1};
+  static const int g[9] = {1, 2, 1, 2, 4, 2, 1, 2, 1};
+  const long n = (long)w * h;
+  std::vector<int16_t> sx(n), sy(n), sxy(n);
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      int16_t ax = 0, ay = 0;
+      for (int oy = -1; oy <= 1; ++oy)
+        for (int ox = -1; ox <= 1; ++ox) {
+          const int rx = remap_idx(bmode, x + ox, 0, w), ry = remap_idx(bmode, y + oy, 0, h);
+          const int v = (rx == kConstIdx || ry == kConstIdx) ? 0 : in[(long)ry * w + rx];
+          const int kx = cx[(oy + 1) * 3 + ox + 1], ky = cy[(oy + 1) * 3 + ox + 1];
+          if (kx) ax = (int16_t)(ax + (int16_t)(v * kx));
+          if (ky) ay = (int16_t)(ay + (int16_t)(v * ky));
+        }
+      const int16_t dx = (int16_t)(ax / 6), dy = (int16_t)(ay / 6);
+      const long p = (long)y * w + x;
+      sx[p] = (int16_t)(dx * dx);
+      sy[p] = (int16_t)(dy * dy);
+      sxy[p] = (int16_t)(dx * dy);
+    }
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      int a = 0, b = 0, c = 0;
+      for (int oy = -1; oy <= 1; ++oy)
+        for (int ox = -1; ox <= 1; ++ox) {
+          const int rx = remap_idx(bmode, x + ox, 0, w), ry = remap_idx(bmode, y + oy, 0, h);
+          const bool cst = rx == kConstIdx || ry == kConstIdx;
+          const long q = cst ? 0 : (long)ry * w + rx;
+          const int m = g[(oy + 1) * 3 + ox + 1];
+          a += (cst ? 0 : sx[q]) * m;
+          b += (cst ? 0 : sy[q]) * m;
+          c += (cst ? 0 : sxy[q]) * m;
+        }
+      const int gx = (int16_t)(a / 16), gy = (int16_t)(b / 16), gxy = (int16_t)(c / 16);
+      const float det = (float)(gx * gy - gxy * gxy);
+      const float tr = (float)(gx + gy);
+      const float kt = k * tr;
+      const float kt2 = kt * tr;
+      const float R = det - kt2;
+      out[(long)y * w + x] = R > threshold ? 1 : 0;
+    }
+}
+
+// Unsharp program (samples-public/1_Local_Operators/Unsharp/src/main.cpp:53-149,203-247,
+// SIZE 3), the blur reading the luminance through the boundary remap:
+//   gray  = (float)((double)(0.2126f * powf(R, c)) + 0.7152 * powf(G, c) + 0.0722 * powf(B, c)),
+//           c = 1.0f / 2.2f (the sample's float and double literals)
+//   blur  = sum_mask gray * m, row-major, products and sums rounded separately
+//   sharp = 2 * gray - blur;  ratio = sharp / max(gray, 0.01f)
+//   out   = (R * ratio, G * ratio, B * ratio, A), each channel the float
+//           product converted to uchar as the CPU back end does: truncated to an
+//           int, low byte kept
+// gray_out (may be NULL) receives the luminance.
+void orc_unsharp_u8x4(const uint8_t *rgba, int w, int h, int bmode, uint8_t *out, float *gray_out, int nthreads) {
+  static const float m[9] = {0.057118f, 0.124758f, 0.057118f, 0.124758f, 0.272496f,
+                             0.124758f, 0.057118f, 0.124758f, 0.057118f};
+  const long n = (long)w * h;
+  std::vector<float> gray(n);
+  const float c = 1.0f / 2.2f;
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+  for (long p = 0; p < n; ++p) {
+    const float xg = powf((float)rgba[4 * p], c), yg = powf((float)rgba[4 * p + 1], c),
+                zg = powf((float)rgba[4 * p + 2], c);
+    const float t0 = 0.2126f * xg;
+    gray[p] = (float)(((double)t0 + 0.7152 * (double)yg) + 0.0722 * (double)zg);
+  }
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      float blur = 0.0f;
+      for (int oy = -1; oy <= 1; ++oy)
+        for (int ox = -1; ox <= 1; ++ox) {
+          const int rx = remap_idx(bmode, x + ox, 0, w), ry = remap_idx(bmode, y + oy, 0, h);
+          const float v = (rx == kConstIdx || ry == kConstIdx) ? 0.0f : gray[(long)ry * w + rx];
+          const float t = m[(oy + 1) * 3 + ox + 1] * v;
+          blur = blur + t;
+        }
+      const long p = (long)y * w + x;
+      const float g2 = 2.0f * gray[p];
+      const float sharp = g2 - blur;
+      const float ratio = sharp / std::max(gray[p], 0.01f);
+      for (int ch = 0; ch < 3; ++ch) {
+        const float v = (float)rgba[4 * p + ch] * ratio;
+        out[4 * p + ch] = (uint8_t)((int32_t)v & 0xff);
+      }
+      out[4 * p + 3] = rgba[4 * p + 3];
+    }
+  if (gray_out) std::copy(gray.begin(), gray.end(), gray_out);
+}
+
 // Adjoint of the bilateral filter in FP64, the forward of
 // samples-public/3_Preprocessing/Bilateral_Filter/src/main.cpp:63-77 (the
 // `bilateral` template above, taps through the boundary remap, CONSTANT taps

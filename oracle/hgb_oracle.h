@@ -120,6 +120,12 @@ void orc_pyramid_collapse_f32(float **out, float **lap, int w, int h, int levels
  * finite differences); `orc_c5_grad_f64` adds the hand adjoint. */
 double orc_c5_loss_f64(const double *x, const double *t, int w, int h, const double *mask, int mk,
                        const double *smask, int sk, double sigma_r, int bmode, int nthreads);
+/* Harris corner program of the Harris_Corner sample (3x3), out 0 / 1. */
+void orc_harris_u8(const uint8_t *in, int w, int h, int bmode, float k, float threshold, uint8_t *out,
+                   int nthreads);
+/* Unsharp program of the Unsharp sample (3x3): uchar4 in and out; gray_out
+ * (may be NULL) receives the luminance image. */
+void orc_unsharp_u8x4(const uint8_t *rgba, int w, int h, int bmode, uint8_t *out, float *gray_out, int nthreads);
 /* Adjoint of the bilateral filter (FP64): dL/din into grad_in (dense w x h) for
  * dL/dy = g; returns dL/dsigma_r. */
 double orc_bilateral_adjoint_f64(const double *in, const double *g, int w, int h, const double *smask, int size,

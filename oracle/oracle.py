@@ -105,6 +105,8 @@ def lib():
         L.orc_bilateral_adjoint_f64.argtypes = [f64p, f64p, C.c_int, C.c_int, f64p, C.c_int, C.c_double, C.c_int,
                                                 C.c_double, f64p]
         L.orc_bilateral_adjoint_f64.restype = C.c_double
+        L.orc_harris_u8.argtypes = [u8p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, u8p, C.c_int]
+        L.orc_unsharp_u8x4.argtypes = [u8p, C.c_int, C.c_int, C.c_int, u8p, C.c_void_p, C.c_int]
         _lib = L
     return _lib
 
@@ -133,6 +135,8 @@ def ref():
             getattr(R, n).argtypes = [f32p, C.c_int, C.c_int]
             getattr(R, n).restype = C.c_float
         R.ref_cpu_red_cores_omp.restype = C.c_int
+        R.ref_harris_u8.argtypes = [u8p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, u8p]
+        R.ref_unsharp_u8x4.argtypes = [u8p, C.c_int, C.c_int, C.c_int, u8p, C.c_void_p]
         R.ref_cpu_interp_f32.argtypes = [C.c_int, f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int]
         for n in ("ref_cpu_histogram_f32_serial", "ref_cpu_histogram_f32_omp"):
             getattr(R, n).argtypes = [f32p, C.c_int, C.c_int, C.c_uint, u32p]
@@ -361,6 +365,28 @@ def c5_grad(x, t, mask, smask, sigma_r, boundary=CLAMP, nthreads=0):
                                  np.ascontiguousarray(smask, np.float64), smask.shape[0], sigma_r, boundary, dx,
                                  dmask, dsig, nt)
     return float(loss), dx, dmask, float(dsig[0])
+
+
+def harris(img, boundary=CLAMP, k=0.04, threshold=20000.0, nthreads=0):
+    """The Harris corner sample's program (3x3): 0 / 1 per pixel."""
+    img = np.ascontiguousarray(img, np.uint8)
+    h, w = img.shape
+    out = np.zeros((h, w), np.uint8)
+    nt = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+    lib().orc_harris_u8(img, w, h, boundary, k, threshold, out, nt)
+    return out
+
+
+def unsharp(rgba, boundary=CLAMP, nthreads=0):
+    """The Unsharp sample's program (3x3): (uchar4 output, luminance)."""
+    rgba = np.ascontiguousarray(rgba, np.uint8)
+    h, w = rgba.shape[:2]
+    out = np.zeros((h, w, 4), np.uint8)
+    gray = np.zeros((h, w), np.float32)
+    nt = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+    lib().orc_unsharp_u8x4(rgba.reshape(h, w * 4), w, h, boundary, out.reshape(h, w * 4), gray.ctypes.data_as(C.c_void_p),
+                           nt)
+    return out, gray
 
 
 def bilateral_adjoint(img, grad_out, smask, sigma_r, boundary=CLAMP, const=0.0):

@@ -15,6 +15,9 @@
 //   bilateral: samples-public/3_Preprocessing/Bilateral_Filter/src/main.cpp:63-77
 //   reduction: samples-public/2_Global_Operators/Reduction_Sum/src/main.cpp:50-62
 //   pyramid:   samples-public/5_Other/Gaussian_Laplacian_Pyramid/src/main.cpp:199-231
+//   Harris:    samples-public/3_Preprocessing/Harris_Corner/src/main.cpp:56-166,258-307 (3x3)
+//   Unsharp:   samples-public/1_Local_Operators/Unsharp/src/main.cpp:53-149,203-247 (3x3)
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -280,9 +283,244 @@ void bilateral_sized(const float *in, int w, int h, const float *coef, float sig
   std::memcpy(out, OUT.data(), sizeof(float) * (size_t)w * h);
 }
 
+// ---- Harris corner sample (3x3): derivative masks over Domains, squares,
+// integer Gaussian with a divisor, response threshold
+class HarrisDerivK : public Kernel<short> {
+  Accessor<uchar> &in;
+  Mask<char> &mask;
+  Domain &dom;
+
+ public:
+  HarrisDerivK(IterationSpace<short> &it, Accessor<uchar> &in, Mask<char> &m, Domain &d)
+      : Kernel(it), in(in), mask(m), dom(d) {
+    add_accessor(&in);
+  }
+  void kernel() {
+    short sum = 0;
+    sum += reduce(dom, Reduce::SUM, [&]() -> short { return in(dom) * mask(dom); });
+    output() = sum / 6;
+  }
+};
+
+class HarrisSq1K : public Kernel<short> {
+  Accessor<short> &in;
+
+ public:
+  HarrisSq1K(IterationSpace<short> &it, Accessor<short> &in) : Kernel(it), in(in) { add_accessor(&in); }
+  void kernel() {
+    short v = in();
+    output() = v * v;
+  }
+};
+
+class HarrisSq2K : public Kernel<short> {
+  Accessor<short> &a, &b;
+
+ public:
+  HarrisSq2K(IterationSpace<short> &it, Accessor<short> &a, Accessor<short> &b) : Kernel(it), a(a), b(b) {
+    add_accessor(&a);
+    add_accessor(&b);
+  }
+  void kernel() { output() = a() * b(); }
+};
+
+class HarrisGaussK : public Kernel<short> {
+  Accessor<short> &in;
+  Mask<uchar> &mask;
+  short norm;
+
+ public:
+  HarrisGaussK(IterationSpace<short> &it, Accessor<short> &in, Mask<uchar> &m, short norm)
+      : Kernel(it), in(in), mask(m), norm(norm) {
+    add_accessor(&in);
+  }
+  void kernel() {
+    int sum = 0;
+    sum += convolve(mask, Reduce::SUM, [&]() -> int { return in(mask) * mask(); });
+    output() = sum / norm;
+  }
+};
+
+class HarrisRespK : public Kernel<uchar> {
+  Accessor<short> &dx, &dy, &dxy;
+  float k, threshold;
+
+ public:
+  HarrisRespK(IterationSpace<uchar> &it, Accessor<short> &dx, Accessor<short> &dy, Accessor<short> &dxy, float k,
+              float threshold)
+      : Kernel(it), dx(dx), dy(dy), dxy(dxy), k(k), threshold(threshold) {
+    add_accessor(&dx);
+    add_accessor(&dy);
+    add_accessor(&dxy);
+  }
+  void kernel() {
+    int x = dx();
+    int y = dy();
+    int xy = dxy();
+    float R = 0;
+    R = ((x * y) - (xy * xy)) - (k * (x + y) * (x + y));
+    uchar out = 0;
+    if (R > threshold) out = 1;
+    output() = out;
+  }
+};
+
+template <typename T>
+BoundaryCondition<T> make_bc_t(Image<T> &img, MaskBase &m, int bmode) {
+  switch (bmode) {
+    case 2: return BoundaryCondition<T>(img, m, Boundary::REPEAT);
+    case 3: return BoundaryCondition<T>(img, m, Boundary::MIRROR);
+    default: return BoundaryCondition<T>(img, m, Boundary::CLAMP);
+  }
+}
+
+// ---- Unsharp sample (3x3): gamma-corrected luminance, blur, sharpen, ratio, scale
+class UnsGrayK : public Kernel<float> {
+  Accessor<uchar4> &in;
+
+ public:
+  UnsGrayK(IterationSpace<float> &it, Accessor<uchar4> &in) : Kernel(it), in(in) { add_accessor(&in); }
+  void kernel() {
+    uchar4 pixel = in();
+    float c = 1.0f / 2.2f;
+    float xg = powf((float)pixel.x, c);
+    float yg = powf((float)pixel.y, c);
+    float zg = powf((float)pixel.z, c);
+    output() = 0.2126f * xg + 0.7152 * yg + 0.0722 * zg;
+  }
+};
+
+class UnsSharpK : public Kernel<float> {
+  Accessor<float> &gray, &blur;
+
+ public:
+  UnsSharpK(IterationSpace<float> &it, Accessor<float> &g, Accessor<float> &b) : Kernel(it), gray(g), blur(b) {
+    add_accessor(&gray);
+    add_accessor(&blur);
+  }
+  void kernel() { output() = 2 * gray() - blur(); }
+};
+
+class UnsRatioK : public Kernel<float> {
+  Accessor<float> &gray, &sharp;
+
+ public:
+  UnsRatioK(IterationSpace<float> &it, Accessor<float> &g, Accessor<float> &s) : Kernel(it), gray(g), sharp(s) {
+    add_accessor(&gray);
+    add_accessor(&sharp);
+  }
+  void kernel() {
+    float pixel = gray();
+    pixel = std::max(pixel, 0.01f);
+    output() = sharp() / pixel;
+  }
+};
+
+class UnsScaleK : public Kernel<uchar4> {
+  Accessor<uchar4> &in;
+  Accessor<float> &ratio;
+
+ public:
+  UnsScaleK(IterationSpace<uchar4> &it, Accessor<uchar4> &in, Accessor<float> &r) : Kernel(it), in(in), ratio(r) {
+    add_accessor(&in);
+    add_accessor(&ratio);
+  }
+  void kernel() {
+    uchar4 v = in();
+    float r = ratio();
+    v.x *= r;
+    v.y *= r;
+    v.z *= r;
+    output() = v;
+  }
+};
+
 }  // namespace
 
 extern "C" {
+
+// The Harris corner program of the sample (3x3 masks, k, threshold) with the
+// boundary bmode (1 CLAMP as the sample, 2 REPEAT, 3 MIRROR) on every local
+// operator; out is 0 / 1 per pixel
+void ref_harris_u8(const uint8_t *input, int w, int h, int bmode, float k, float threshold, uint8_t *out) {
+  const short norm = 16;
+  const uchar cxy[3][3] = {{1, 2, 1}, {2, 4, 2}, {1, 2, 1}};
+  const char cx[3][3] = {{-1, 0, 1}, {-1, 0, 1}, {-1, 0, 1}};
+  const char cy[3][3] = {{-1, -1, -1}, {0, 0, 0}, {1, 1, 1}};
+  Image<uchar> IN(w, h, const_cast<uint8_t *>(input));
+  Image<uchar> OUT(w, h);
+  Image<short> dx(w, h), dy(w, h), dxy(w, h), sx(w, h), sy(w, h), sxy(w, h);
+  Mask<uchar> maskxy(cxy);
+  Mask<char> maskx(cx), masky(cy);
+  Domain domx(maskx), domy(masky);
+  IterationSpace<short> iter_dx(dx), iter_dy(dy), iter_sx(sx), iter_sy(sy), iter_sxy(sxy), iter_dxy(dxy);
+  BoundaryCondition<uchar> bound_in = make_bc_t<uchar>(IN, maskx, bmode);
+  Accessor<uchar> acc_in(bound_in);
+  HarrisDerivK derivx(iter_dx, acc_in, maskx, domx);
+  derivx.execute();
+  HarrisDerivK derivy(iter_dy, acc_in, masky, domy);
+  derivy.execute();
+  Accessor<short> acc_dx(dx), acc_dy(dy);
+  HarrisSq1K squarex(iter_sx, acc_dx);
+  squarex.execute();
+  HarrisSq1K squarey(iter_sy, acc_dy);
+  squarey.execute();
+  HarrisSq2K squarexy(iter_sxy, acc_dx, acc_dy);
+  squarexy.execute();
+  BoundaryCondition<short> bound_sx = make_bc_t<short>(sx, maskxy, bmode);
+  Accessor<short> acc_sx(bound_sx);
+  HarrisGaussK gaussx(iter_dx, acc_sx, maskxy, norm);
+  gaussx.execute();
+  BoundaryCondition<short> bound_sy = make_bc_t<short>(sy, maskxy, bmode);
+  Accessor<short> acc_sy(bound_sy);
+  HarrisGaussK gaussy(iter_dy, acc_sy, maskxy, norm);
+  gaussy.execute();
+  BoundaryCondition<short> bound_sxy = make_bc_t<short>(sxy, maskxy, bmode);
+  Accessor<short> acc_sxy(bound_sxy);
+  HarrisGaussK gaussxy(iter_dxy, acc_sxy, maskxy, norm);
+  gaussxy.execute();
+  IterationSpace<uchar> iter_out(OUT);
+  Accessor<short> acc_dxy(dxy);
+  HarrisRespK harris(iter_out, acc_dx, acc_dy, acc_dxy, k, threshold);
+  harris.execute();
+  std::memcpy(out, OUT.data(), (size_t)w * h);
+}
+
+// The Unsharp program of the sample (3x3 mask) with the blur's boundary bmode;
+// gray_out (may be NULL) receives the luminance image
+void ref_unsharp_u8x4(const uint8_t *rgba, int w, int h, int bmode, uint8_t *out, float *gray_out) {
+  const float coef[3][3] = {{0.057118f, 0.124758f, 0.057118f},
+                            {0.124758f, 0.272496f, 0.124758f},
+                            {0.057118f, 0.124758f, 0.057118f}};
+  Image<uchar4> IN(w, h, reinterpret_cast<uchar4 *>(const_cast<uint8_t *>(rgba)));
+  Image<float> gray(w, h), blur(w, h), sharp(w, h), ratio(w, h);
+  Image<uchar4> OUT(w, h);
+  Mask<float> mask(coef);
+  IterationSpace<float> iterGray(gray);
+  Accessor<uchar4> accIn(IN);
+  UnsGrayK g(iterGray, accIn);
+  g.execute();
+  BoundaryCondition<float> bound = make_bc_t<float>(gray, mask, bmode);
+  Accessor<float> accGrayBound(bound);
+  Accessor<float> accGray(gray);
+  IterationSpace<float> iterBlur(blur);
+  ConvK gb(iterBlur, accGrayBound, mask);
+  gb.execute();
+  IterationSpace<float> iterSharp(sharp);
+  Accessor<float> accBlur(blur);
+  UnsSharpK sh(iterSharp, accGray, accBlur);
+  sh.execute();
+  IterationSpace<float> iterRatio(ratio);
+  Accessor<float> accSharp(sharp);
+  UnsRatioK ra(iterRatio, accGray, accSharp);
+  ra.execute();
+  IterationSpace<uchar4> iter(OUT);
+  Accessor<float> accRatio(ratio);
+  UnsScaleK us(iter, accIn, accRatio);
+  us.execute();
+  std::memcpy(out, OUT.data(), (size_t)w * h * 4);
+  if (gray_out) std::memcpy(gray_out, gray.data(), sizeof(float) * (size_t)w * h);
+}
 
 // returns 0 on success, -1 for an unsupported mask size
 int ref_conv_f32(const float *in, int w, int h, const float *coef, int mw, int mh, int bmode, int dom_mode,

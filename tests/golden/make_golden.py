@@ -12,6 +12,7 @@ compiled with -ffp-contract=off (no fused multiply-add).
 """
 from __future__ import annotations
 
+import ctypes as C
 import os
 import sys
 
@@ -20,6 +21,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
 import oracle as O  # noqa: E402
+
+
+def blocks_u8(rng, h, w, n=12, noise=6):
+    """Random axis-aligned rectangles of random grey levels plus uniform noise."""
+    img = np.full((h, w), int(rng.integers(0, 256)), np.int32)
+    for _ in range(n):
+        y0, x0 = int(rng.integers(0, h - 2)), int(rng.integers(0, w - 2))
+        y1, x1 = int(rng.integers(y0 + 2, h + 1)), int(rng.integers(x0 + 2, w + 1))
+        img[y0:y1, x0:x1] = int(rng.integers(0, 256))
+    img += rng.integers(-noise, noise + 1, (h, w))
+    return np.clip(img, 0, 255).astype(np.uint8)
 
 
 def main():
@@ -138,6 +150,21 @@ def main():
         out[f"domain_u8_r{red}_in"] = img
         out[f"domain_u8_r{red}_dom"] = dom.astype(np.uint8)
         out[f"domain_u8_r{red}_out"] = r
+    # the Harris corner and Unsharp sample programs (3x3) on structured images:
+    # random rectangles plus noise give corners, edges and flat regions
+    for b in (O.CLAMP, O.REPEAT, O.MIRROR):
+        img = blocks_u8(rng, 40, 56)
+        r = np.zeros_like(img)
+        R.ref_harris_u8(img, 56, 40, b, 0.04, 20000.0, r)
+        out[f"harris_b{b}_in"] = img
+        out[f"harris_b{b}_out"] = r
+        rgba = np.stack([blocks_u8(rng, 33, 47) for _ in range(4)], axis=-1)
+        ro = np.zeros_like(rgba)
+        rg = np.zeros((33, 47), np.float32)
+        R.ref_unsharp_u8x4(rgba.reshape(33, 47 * 4), 47, 33, b, ro.reshape(33, 47 * 4), rg.ctypes.data_as(C.c_void_p))
+        out[f"unsharp_b{b}_in"] = rgba
+        out[f"unsharp_b{b}_out"] = ro
+        out[f"unsharp_b{b}_gray"] = rg
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path), "bytes,", len(out), "arrays")
 

@@ -4,7 +4,9 @@ the FP64 oracle's hand adjoint (itself pinned to FP64 central differences in
 test_oracle_adjoint.py) and against FP64 central differences (eps = 1e-4) of
 the FP64 forward on 64x64 crops.  The kernels evaluate the range weights with
 the FP32 exp2 instruction and accumulate in FP32, so gradients agree with FP64
-to ADJ_TOL relative (L2 norm over the image) and dL/dsigma_r to ADJ_TOL."""
+to ADJ_TOL relative (L2 norm over the image) and dL/dsigma_r to ADJ_TOL
+relative, with an absolute floor of SIGMA_ABS where its terms cancel to a
+small total (FP32 sums of terms of both signs)."""
 import numpy as np
 import pytest
 import torch
@@ -12,6 +14,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 ADJ_TOL = 2e-3
+SIGMA_ABS = 1e-4
 FD_TOL = 5e-3
 
 
@@ -42,7 +45,7 @@ def test_bilateral_adjoint_vs_fp64_oracle(gpu, oracle, boundary, const, size, hw
         ref_gi.append(a)
         ref_gs += s
     assert rel(gi, np.stack(ref_gi)) <= ADJ_TOL, rel(gi, np.stack(ref_gi))
-    assert abs(gs - ref_gs) <= ADJ_TOL * abs(ref_gs), (gs, ref_gs)
+    assert abs(gs - ref_gs) <= max(ADJ_TOL * abs(ref_gs), SIGMA_ABS), (gs, ref_gs)
 
 
 @pytest.mark.parametrize("boundary", [1, 3])
@@ -79,7 +82,8 @@ def test_bilateral_adjoint_asymmetric_mask(gpu, oracle):
     for boundary in (1, 2, 3):
         gi, gs = _gpu(gpu, x, g, sm, 0.2, boundary, 0.0)
         a, s = oracle.bilateral_adjoint(x[0], g[0], sm.astype(np.float64), 0.2, boundary, 0.0)
-        assert rel(gi[0], a) <= ADJ_TOL and abs(gs - s) <= ADJ_TOL * abs(s), boundary
+        assert rel(gi[0], a) <= ADJ_TOL, boundary
+        assert abs(gs - s) <= max(ADJ_TOL * abs(s), SIGMA_ABS), (boundary, gs, s)
 
 
 def test_bilateral_adjoint_partial_requests_and_errors(gpu, oracle):
@@ -97,7 +101,7 @@ def test_bilateral_adjoint_partial_requests_and_errors(gpu, oracle):
     with pytest.raises(L.HgbError):
         gpu.bilateral_adjoint(x, g, sm, 0.1, 3, want_grad_in=False, want_grad_sigma=False)
     with pytest.raises(L.HgbError):
-        gpu.bilateral_adjoint(x, g, oracle.spatial_mask(4, 1.0), 0.1, 3)
+        gpu.bilateral_adjoint(x, g, np.ones((4, 4), np.float32), 0.1, 3)
     with pytest.raises(L.HgbError):
         gpu.bilateral_adjoint(x, g, sm, -0.1, 3)
 

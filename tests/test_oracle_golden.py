@@ -177,9 +177,29 @@ def test_live_reference_pin(oracle, b):
         assert R.ref_conv_u8(img, 37, 29, dom, 5, 5, b, 1, red, r) == 0
         got = O.local_op_u8(img, domain=dom.astype(np.uint8), size=(5, 5), reduce=red, boundary=b, contract=0)
         assert np.array_equal(got, r), red
+    if b != O.CONSTANT:  # the programs' DSL runs honour CLAMP / REPEAT / MIRROR
+        img = rng.integers(0, 256, (35, 44), dtype=np.uint8)
+        r = np.zeros_like(img)
+        R.ref_harris_u8(img, 44, 35, b, 0.04, 20000.0, r)
+        assert np.array_equal(O.harris(img, b), r)
+        rgba = rng.integers(0, 256, (27, 31, 4), dtype=np.uint8)
+        ro = np.zeros_like(rgba)
+        R.ref_unsharp_u8x4(rgba.reshape(27, 31 * 4), 31, 27, b, ro.reshape(27, 31 * 4), None)
+        assert np.array_equal(O.unsharp(rgba, b)[0], ro)
     f = rng.random((40, 52), dtype=np.float32)
     nc = R.ref_cpu_red_cores_omp()
     assert np.float32(R.ref_cpu_red_sum_f32_omp(f, 52, 40)) == np.float32(O.reduce_f32(f, O.SUM, nc))
+
+
+def test_harris_unsharp_golden(oracle, golden):
+    """The Harris corner and Unsharp sample programs as the reference's DSL ran
+    them: bit-exact, luminance included."""
+    O = oracle
+    for b in (O.CLAMP, O.REPEAT, O.MIRROR):
+        assert np.array_equal(O.harris(golden[f"harris_b{b}_in"], b), golden[f"harris_b{b}_out"]), b
+        o, g = O.unsharp(golden[f"unsharp_b{b}_in"], b)
+        assert np.array_equal(o, golden[f"unsharp_b{b}_out"]), b
+        assert np.array_equal(g, golden[f"unsharp_b{b}_gray"]), b
 
 
 def test_adjoint_oracle_matches_finite_differences(oracle):

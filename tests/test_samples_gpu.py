@@ -9,7 +9,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-SAMPLES = ["gaussian_blur", "sobel", "color_reduce", "pyramid", "bilateral", "graph"]
+SAMPLES = ["gaussian_blur", "sobel", "color_reduce", "pyramid", "bilateral", "graph", "pipelines"]
 
 
 @pytest.fixture(scope="module")
