@@ -410,7 +410,7 @@ def gauss_taps(k, sigma):
     return (g / g.sum()).astype(np.float32)
 
 
-OTHER_SECTIONS = ("integer", "gaussian", "precision", "pyramid", "diff", "histogram", "pipelines")
+OTHER_SECTIONS = ("integer", "gaussian", "precision", "pyramid", "diff", "histogram", "pipelines", "extras")
 
 
 def measure_other_configs(dev, peak_gbs, only=None):
@@ -441,6 +441,8 @@ def measure_other_configs(dev, peak_gbs, only=None):
         _histogram(dev, peak_gbs, s, res, q)
     if want("pipelines"):
         _pipelines(dev, peak_gbs, s, res, q)
+    if want("extras"):
+        _extras(dev, peak_gbs, s, res, q)
     return res
 
 
@@ -464,6 +466,54 @@ def _integer(dev, peak_gbs, s, res):
     us = graph_time_us(lambda i: api.gray(rgbas[i], grays[i], stream=s), n, s, 2)
     res["rgba_gray_4096"] = {"us_per_launch": us, "achieved_gbs": GRAY_BYTES / us / 1e3,
                              "frac_hbm": GRAY_BYTES / us / 1e3 / peak_gbs}
+
+
+def _extras(dev, peak_gbs, s, res, q):
+    """The remaining operators of the path, each alone: standalone global reductions, resampling
+    accessors, and the two adjoints.  Rotating inputs larger than L2."""
+    import torch
+
+    from hipacc_gb300 import api
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(17)
+    n, px = 8, 4096 * 4096
+    reps = 1 if q else 10
+    u8 = [torch.randint(0, 256, (4096, 4096), dtype=torch.uint8, device=dev, generator=g) for _ in range(n)]
+    r8 = torch.zeros(n, dtype=torch.int64, device=dev)
+    us = graph_time_us(lambda i: api.L.call("hgb_reduce", C.byref(api.view(u8[i])), None, api.SUM,
+                                            C.c_void_p(r8[i:i + 1].data_ptr()), None, api._stream(s)), n, s, reps)
+    res["reduce_sum_u8_u64_4096"] = {"us_per_launch": us, "gpix_s": px / us / 1e3, "achieved_gbs": px / us / 1e3,
+                                     "frac_hbm": px / us / 1e3 / peak_gbs}
+    del u8
+    f32 = [torch.rand((4096, 4096), device=dev, generator=g) for _ in range(n)]
+    rf = torch.zeros(n, dtype=torch.float64, device=dev)
+    us = graph_time_us(lambda i: api.L.call("hgb_reduce", C.byref(api.view(f32[i])), None, api.SUM,
+                                            C.c_void_p(rf[i:i + 1].data_ptr()), None, api._stream(s)), n, s, reps)
+    res["reduce_sum_f32_kahan_4096"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                        "achieved_gbs": 4 * px / us / 1e3, "frac_hbm": 4 * px / us / 1e3 / peak_gbs}
+    # resampling accessors: 2048^2 -> 4096^2 (4 bytes read per output / 4 plus 4 written)
+    src = [torch.rand((2048, 2048), device=dev, generator=g) for _ in range(n)]
+    dst = [torch.empty((4096, 4096), device=dev) for _ in range(n)]
+    for mode in ("nn", "lf", "b5", "cf", "l3"):
+        us = graph_time_us(lambda i: api.resample(src[i], dst[i], mode, stream=s), n, s, reps)
+        b = 4 * px + 4 * px // 4
+        res[f"resample_{mode}_2048_to_4096"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                                "achieved_gbs": b / us / 1e3, "frac_hbm": b / us / 1e3 / peak_gbs}
+    del src, dst
+    # adjoints: 7x7 SUM local operator (grad_in + grad_mask) and 9x9 bilateral (grad_in + grad_sigma)
+    gout = [torch.randn((4096, 4096), device=dev, generator=g) for _ in range(n)]
+    m7 = np.random.default_rng(3).normal(0, 0.1, (7, 7)).astype(np.float32)
+    us = graph_time_us(lambda i: api.local_op_adjoint(gout[i], m7, api.CLAMP, inp=f32[i], stream=s), n, s, reps)
+    res["local_op_adjoint7_f32_4096"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                         "achieved_gbs": 12 * px / us / 1e3, "frac_hbm": 12 * px / us / 1e3 / peak_gbs}
+    ax = np.arange(-4, 5, dtype=np.float64)
+    sm9 = np.exp(-(ax[None, :] ** 2 + ax[:, None] ** 2) / (2 * 4.0)).astype(np.float32)
+    us = graph_time_us(lambda i: api.bilateral_adjoint(f32[i], gout[i], sm9, 0.15, api.CLAMP, stream=s), n, s,
+                       max(1, reps // 5))
+    res["bilateral_adjoint9_f32_4096"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
+                                          "exp_per_s": 2 * 81 * px / us * 1e6}
+    del gout, f32
 
 
 def _pipelines(dev, peak_gbs, s, res, q):
@@ -575,7 +625,45 @@ def _precision(dev, peak_gbs, s, res, q):
             res[f"bilateral13_{name}_halfweights_8192_repeat"] = {"us_per_launch": us, "gpix_s": px / us / 1e3,
                                                                   "exp_per_s": 169 * px / us * 1e6}
         del ins, outs
+    res["precision_error_vs_fp64"] = _precision_errors(img32[0], taps, sm)
     del img32
+
+
+def _err(got, ref):
+    """max-abs and max-relative (max-abs / max |ref|) error of got against an FP64 reference."""
+    got = np.asarray(got, np.float64)
+    d = float(np.max(np.abs(got - ref)))
+    return {"max_abs": d, "max_rel": d / max(float(np.max(np.abs(ref))), 1e-300)}
+
+
+def _precision_errors(img, taps, sm):
+    """Error of each storage type against the FP64 oracle, outside the timed region: the same kernels on
+    the 512 x 512 corner crop of the benchmarked field (as a whole image, so both borders and interior
+    count), against FP64 on the FP32 crop (input rounding of BF16 / FP16 storage included)."""
+    import torch
+
+    from hipacc_gb300 import api
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    crop = img[:512, :512].contiguous()
+    c64 = crop.double().cpu().numpy()
+    out = {}
+    for b, bname in ((api.REPEAT, "repeat"), (api.CONSTANT, "constant0.5")):
+        ref_sep = O.separable(c64, taps.astype(np.float64), taps.astype(np.float64), boundary=b, const=0.5)
+        ref_bil = O.bilateral(c64, sm.astype(np.float64), 0.1, boundary=b, const=0.5)
+        for name, dt in (("f32", torch.float32), ("bf16", torch.bfloat16), ("f16", torch.float16)):
+            x = crop.to(dt)
+            y = api.separable(x, None, taps, taps, boundary=b, const=0.5)
+            out[f"separable9_{name}_{bname}"] = _err(y.double().cpu().numpy(), ref_sep)
+            y = api.bilateral(x, None, sm, 0.1, boundary=b, const=0.5)
+            out[f"bilateral13_{name}_{bname}"] = _err(y.double().cpu().numpy(), ref_bil)
+            if dt != torch.float32:
+                y = api.bilateral(x, None, sm, 0.1, boundary=b, const=0.5, fast_weights=True)
+                out[f"bilateral13_{name}_halfweights_{bname}"] = _err(y.double().cpu().numpy(), ref_bil)
+    torch.cuda.synchronize()
+    return out
 
 
 def _pyramid(dev, peak_gbs, s, res, q):
@@ -603,6 +691,22 @@ def _pyramid(dev, peak_gbs, s, res, q):
         us = graph_time_us(lambda i: plan.decompose(mode, stream=s), 1, s, 1 if q else (3 if mode < 2 else 2))
         res[f"pyramid8_64img_{name}"] = {"us_per_batch": us, "gpix_s": base_px / us / 1e3,
                                          "achieved_gbs": alg / us / 1e3, "frac_hbm": alg / us / 1e3 / peak_gbs}
+    # error of the persistent form's levels against the FP64 oracle, outside the timed region: the
+    # smallest image of the batch, every level
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    plan.decompose(0, stream=s)
+    torch.cuda.synchronize()
+    i = int(np.argmin(ws_.astype(np.int64) * hs_))
+    g64, l64 = O.pyramid_decompose(plan.gauss(i, 0).double().cpu().numpy(), levels, b1[:, None] * b1[None, :],
+                                   O.MIRROR)
+    err = {"image": f"{int(ws_[i])}x{int(hs_[i])}"}
+    for l in range(levels):
+        err[f"gauss{l}"] = _err(plan.gauss(i, l).double().cpu().numpy(), g64[l])
+        if l + 1 < levels:
+            err[f"lap{l}"] = _err(plan.lap(i, l).double().cpu().numpy(), l64[l])
+    res["pyramid8_error_vs_fp64"] = err
     plan.close()
 
 
@@ -629,6 +733,22 @@ def _diff(dev, s, res, q):
         us = graph_time_us(lambda i: api.conv_bilateral_mse(x, t, mask, sigma, sm9, api.CLAMP, mode, stream=s), 1, s,
                            1 if q else 3)
         res[f"conv7_bilateral9_mse_fwd_adj_16x2048_{name}"] = {"us_per_batch": us, "gpix_s": px / us / 1e3}
+    # error against the FP64 oracle's forward + hand adjoint (pinned to FP64 central differences by the
+    # tests), outside the timed region: image 0 of the batch as its own launch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    loss, gx, gm, gs = api.conv_bilateral_mse(x[0:1], t[0:1], mask, sigma, sm9, api.CLAMP, 0, stream=s)
+    torch.cuda.synchronize()
+    l0, dx0, dm0, ds0 = O.c5_grad(x[0].cpu().numpy(), t[0].cpu().numpy(), mask.double().cpu().numpy(),
+                                  sm9.astype(np.float64), 0.15, O.CLAMP)
+    rel = lambda a, b: float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300))
+    res["conv7_bilateral9_mse_error_vs_fp64"] = {
+        "image": "2048x2048 (image 0 of the batch), CLAMP",
+        "loss_rel": abs(float(loss.item()) - l0) / abs(l0),
+        "grad_x_rel_l2": rel(gx[0].double().cpu().numpy(), dx0),
+        "grad_mask_rel_l2": rel(gm.double().cpu().numpy(), dm0),
+        "grad_sigma_rel": abs(float(gs.item()) - ds0) / abs(ds0)}
     del x, t
 
 
