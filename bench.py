@@ -687,10 +687,22 @@ def _pyramid(dev, peak_gbs, s, res, q):
         for _ in range(levels - 1):
             alg += 8.0 * w * h + 4.0 * (w // 2) * (h // 2)  # read G_l, write L_l, write G_{l+1}
             w, h = w // 2, h // 2
+    # the fused launch forms pick their tile configuration with the autotuner (first, untimed call)
+    api.autotune(True)
     for mode, name in ((0, "persistent_1launch"), (1, "per_level_7launches"), (2, "per_image_per_level_1344launches")):
         us = graph_time_us(lambda i: plan.decompose(mode, stream=s), 1, s, 1 if q else (3 if mode < 2 else 2))
         res[f"pyramid8_64img_{name}"] = {"us_per_batch": us, "gpix_s": base_px / us / 1e3,
                                          "achieved_gbs": alg / us / 1e3, "frac_hbm": alg / us / 1e3 / peak_gbs}
+    api.autotune(False)
+    import tempfile
+
+    tuned = os.path.join(tempfile.gettempdir(), f"hgb_pyramid_autotune_{os.getpid()}.json")
+    try:
+        api.L.call("hgb_autotune_save", tuned.encode())
+        res["pyramid8_autotuned_choices"] = {k: v for k, v in json.load(open(tuned)).items() if k.startswith("pyramid")}
+        os.remove(tuned)
+    except (OSError, ValueError):
+        pass
     # error of the persistent form's levels against the FP64 oracle, outside the timed region: the
     # smallest image of the batch, every level
     sys.path.insert(0, os.path.join(ROOT, "oracle"))

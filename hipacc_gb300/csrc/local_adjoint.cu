@@ -21,6 +21,7 @@ namespace {
 constexpr int LA_TW = 32, LA_TH = 16, LA_T = 256, LA_MAX = 15;
 constexpr int LA_SW = LA_TW + 2 * LA_MAX, LA_SH = LA_TH + 2 * LA_MAX;
 constexpr int LA_ROWBLOCKS = 64;
+constexpr int LM_TW = 64, LM_TH = 16, LM_PX = 4;  // tiles of the square-mask kernels
 
 struct AdjParams {
   const float *in, *gout;
@@ -96,6 +97,71 @@ __global__ void __launch_bounds__(LA_T) adj_in_kernel(const __grid_constant__ Ad
   }
 }
 
+// Square K x K masks: grad_in on a 64 x 16 tile, a thread per four
+// consecutive pixels of a row.  Inside the image (every pixel at least the
+// radius from the border) grad_in(i) = sum_o m_o grad_out(i - o): each staged
+// row value serves all taps that read it.  Pixels near the border gather over
+// their pre-images as adj_in_kernel does.
+template <int K>
+__global__ void __launch_bounds__(LA_T) adj_in_tile_kernel(const __grid_constant__ AdjParams p) {
+  constexpr int R = K / 2, SW = LM_TW + 2 * R, SH = LM_TH + 2 * R;
+  __shared__ float sg[SH * SW];
+  __shared__ float msk[K * K];
+  const int b = blockIdx.z, X0 = blockIdx.x * LM_TW, Y0 = blockIdx.y * LM_TH;
+  const float *gout = p.gout + (int64_t)b * p.gout_b;
+  for (int k = threadIdx.x; k < K * K; k += LA_T) msk[k] = p.mask_dev ? __ldg(p.mask_dev + k) : p.mask[k];
+  for (int c = threadIdx.x; c < SH * SW; c += LA_T) {
+    const int r = c / SW, q = c - r * SW;
+    const int gy = Y0 - R + r, gx = X0 - R + q;
+    sg[c] = (gx >= 0 && gx < p.w && gy >= 0 && gy < p.h) ? __ldg(gout + (int64_t)gy * p.gout_p + gx) : 0.0f;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % (LM_TW / LM_PX), ty = threadIdx.x / (LM_TW / LM_PX);
+  const int x = X0 + tx * LM_PX, y = Y0 + ty;
+  if (y >= p.h || x >= p.w) return;
+  float acc[LM_PX];
+#pragma unroll
+  for (int q = 0; q < LM_PX; ++q) acc[q] = 0.0f;
+  const bool inner = x >= R && x + LM_PX - 1 < p.w - R && y >= R && y < p.h - R;
+  if (inner) {
+    // taps in the order of adj_in_kernel: my, then mx ascending; j = i - o
+#pragma unroll
+    for (int my = 0; my < K; ++my) {
+      const float *row = &sg[(ty + 2 * R - my) * SW + tx * LM_PX];  // grad_out row y - (my - R)
+      float v[LM_PX + K - 1];
+#pragma unroll
+      for (int i = 0; i < LM_PX + K - 1; ++i) v[i] = row[i];
+#pragma unroll
+      for (int mx = 0; mx < K; ++mx)
+#pragma unroll
+        for (int q = 0; q < LM_PX; ++q)  // column x + q - (mx - R): v[q + 2R - mx]
+          acc[q] = __fmaf_rn(msk[my * K + mx], v[q + 2 * R - mx], acc[q]);
+    }
+  } else {
+    for (int q = 0; q < LM_PX; ++q) {
+      const int ix = x + q;
+      if (ix >= p.w) break;
+      int prx[2 * LA_MAX + 1], pry[2 * LA_MAX + 1];
+      const int nx = pre_list(p.bmode, ix, p.w, R + 1, R + 1, prx);
+      const int ny = pre_list(p.bmode, y, p.h, R + 1, R + 1, pry);
+      float a = 0.0f;
+      for (int ia = 0; ia < ny; ++ia)
+        for (int ic = 0; ic < nx; ++ic)
+          for (int my = 0; my < K; ++my)
+            for (int mx = 0; mx < K; ++mx) {
+              const int jy = pry[ia] - (my - R), jx = prx[ic] - (mx - R);
+              if (jx < 0 || jx >= p.w || jy < 0 || jy >= p.h) continue;
+              a = __fmaf_rn(msk[my * K + mx], __ldg(gout + (int64_t)jy * p.gout_p + jx), a);
+            }
+      acc[q] = a;
+    }
+  }
+  float *gin = p.gin + (int64_t)b * p.gin_b + (int64_t)y * p.gin_p;
+#pragma unroll
+  for (int q = 0; q < LM_PX; ++q)
+    if (x + q < p.w) gin[x + q] = acc[q];
+}
+
 // grid (taps, LA_ROWBLOCKS, batch): partial of grad_m(o) over a band of rows
 __global__ void __launch_bounds__(LA_T) adj_mask_kernel(const __grid_constant__ AdjParams p) {
   const int o = blockIdx.x, b = blockIdx.z;
@@ -125,12 +191,78 @@ __global__ void __launch_bounds__(LA_T) adj_mask_kernel(const __grid_constant__ 
   }
 }
 
-__global__ void adj_mask_combine(const __grid_constant__ AdjParams p, int nparts) {
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= p.mw * p.mh) return;
+// Square K x K masks: one CTA per 64 x 16 tile of grad_out accumulates every
+// tap's partial at once.  The input region the tile's taps read is staged once
+// (through the boundary remap; CONSTANT taps read 0, which adds nothing), a
+// thread owns four consecutive pixels of a row and keeps the K * K partials in
+// registers, reusing each staged value for all taps that read it.  Per-CTA
+// partials [cta][tap] are combined in FP64 in a fixed order.
+template <int K>
+__global__ void __launch_bounds__(LA_T) adj_mask_tile_kernel(const __grid_constant__ AdjParams p) {
+  constexpr int R = K / 2, SW = LM_TW + 2 * R, SH = LM_TH + 2 * R;
+  __shared__ float s_in[SH * SW];
+  __shared__ float s_red[LA_T / 32][K * K];
+  const int b = blockIdx.z, X0 = blockIdx.x * LM_TW, Y0 = blockIdx.y * LM_TH;
+  const float *in = p.in + (int64_t)b * p.in_b;
+  const float *gout = p.gout + (int64_t)b * p.gout_b;
+  for (int c = threadIdx.x; c < SH * SW; c += LA_T) {
+    const int r = c / SW, q = c - r * SW;
+    const int ry = remap(p.bmode, Y0 - R + r, 0, p.h), rx = remap(p.bmode, X0 - R + q, 0, p.w);
+    s_in[c] = (ry == (int)0x80000000 || rx == (int)0x80000000) ? 0.0f : __ldg(in + (int64_t)ry * p.in_p + rx);
+  }
+  const int tx = threadIdx.x % (LM_TW / LM_PX), ty = threadIdx.x / (LM_TW / LM_PX);
+  const int x = X0 + tx * LM_PX, y = Y0 + ty;
+  float g[LM_PX];
+#pragma unroll
+  for (int q = 0; q < LM_PX; ++q)
+    g[q] = (y < p.h && x + q < p.w) ? __ldg(gout + (int64_t)y * p.gout_p + x + q) : 0.0f;
+  __syncthreads();
+  float dm[K * K];
+#pragma unroll
+  for (int i = 0; i < K * K; ++i) dm[i] = 0.0f;
+#pragma unroll
+  for (int my = 0; my < K; ++my) {
+    const float *row = &s_in[(ty + my) * SW + tx * LM_PX];
+    float v[LM_PX + K - 1];
+#pragma unroll
+    for (int i = 0; i < LM_PX + K - 1; ++i) v[i] = row[i];
+#pragma unroll
+    for (int mx = 0; mx < K; ++mx)
+#pragma unroll
+      for (int q = 0; q < LM_PX; ++q) dm[my * K + mx] = __fmaf_rn(g[q], v[q + mx], dm[my * K + mx]);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < K * K; ++i) {
+    float t = dm[i];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) t += __shfl_down_sync(0xffffffffu, t, d);
+    if (lane == 0) s_red[warp][i] = t;
+  }
+  __syncthreads();
+  const unsigned cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  const unsigned ncta = gridDim.x * gridDim.y * gridDim.z;
+  for (int i = threadIdx.x; i < K * K; i += LA_T) {
+    float t = 0.0f;
+    for (int w = 0; w < LA_T / 32; ++w) t += s_red[w][i];
+    p.part[(size_t)i * ncta + cta] = t;
+  }
+}
+
+// one CTA per tap: thread t folds partials t, t + LA_T, ... in FP64, then a
+// fixed tree over the threads (the same order on every run)
+__global__ void __launch_bounds__(LA_T) adj_mask_combine(const __grid_constant__ AdjParams p, int nparts) {
+  __shared__ double sh[LA_T];
+  const int o = blockIdx.x;
   double s = 0.0;
-  for (int k = 0; k < nparts; ++k) s += (double)p.part[(size_t)o * nparts + k];
-  p.grad_mask_dev[o] = (float)s;
+  for (int k = threadIdx.x; k < nparts; k += LA_T) s += (double)p.part[(size_t)o * nparts + k];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int d = LA_T / 2; d > 0; d >>= 1) {
+    if (threadIdx.x < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) p.grad_mask_dev[o] = (float)sh[0];
 }
 
 }  // namespace
@@ -191,16 +323,34 @@ extern "C" int hgb_local_op_adjoint(const hgb_view *in, const hgb_view *grad_out
   cudaStream_t st = (cudaStream_t)stream;
   cudaEvent_t ev = before_launch(st);
   if (grad_in) {
-    adj_in_kernel<<<dim3(cdiv(p.w, LA_TW), cdiv(p.h, LA_TH), p.batch), LA_T, 0, st>>>(p);
+    const dim3 tg(cdiv(p.w, LM_TW), cdiv(p.h, LM_TH), p.batch);
+    if (mask_w == mask_h && mask_w == 3)
+      adj_in_tile_kernel<3><<<tg, LA_T, 0, st>>>(p);
+    else if (mask_w == mask_h && mask_w == 5)
+      adj_in_tile_kernel<5><<<tg, LA_T, 0, st>>>(p);
+    else if (mask_w == mask_h && mask_w == 7)
+      adj_in_tile_kernel<7><<<tg, LA_T, 0, st>>>(p);
+    else
+      adj_in_kernel<<<dim3(cdiv(p.w, LA_TW), cdiv(p.h, LA_TH), p.batch), LA_T, 0, st>>>(p);
   }
   if (grad_mask_dev) {
-    const int taps = mask_w * mask_h, nparts = LA_ROWBLOCKS * p.batch;
+    const int taps = mask_w * mask_h;
+    const bool tiled = mask_w == mask_h && (mask_w == 3 || mask_w == 5 || mask_w == 7);
+    const dim3 tg(cdiv(p.w, LM_TW), cdiv(p.h, LM_TH), p.batch);
+    const int nparts = tiled ? (int)(tg.x * tg.y * tg.z) : LA_ROWBLOCKS * p.batch;
     Workspace ws;
     rc = workspace_get((size_t)taps * nparts * 4 + 64, &ws);
     if (rc) return rc;
     p.part = (float *)ws.base;
-    adj_mask_kernel<<<dim3(taps, LA_ROWBLOCKS, p.batch), LA_T, 0, st>>>(p);
-    adj_mask_combine<<<cdiv(taps, 128), 128, 0, st>>>(p, nparts);
+    if (!tiled)
+      adj_mask_kernel<<<dim3(taps, LA_ROWBLOCKS, p.batch), LA_T, 0, st>>>(p);
+    else if (mask_w == 3)
+      adj_mask_tile_kernel<3><<<tg, LA_T, 0, st>>>(p);
+    else if (mask_w == 5)
+      adj_mask_tile_kernel<5><<<tg, LA_T, 0, st>>>(p);
+    else
+      adj_mask_tile_kernel<7><<<tg, LA_T, 0, st>>>(p);
+    adj_mask_combine<<<taps, LA_T, 0, st>>>(p, nparts);
   }
   return after_launch("local_op_adjoint", st, ev);
 }

@@ -255,58 +255,98 @@ __device__ __forceinline__ float wt_l3(float d) {
   return 0.0f;
 }
 
-__device__ float filtered_sample(const float *src, int64_t sp, int sw, int sh, float xm, float ym, int imode) {
+// Tap tables of the filtered modes, per output column and per output row: the
+// first tap index and the n weights (the weights depend only on the column or
+// the row, so each is evaluated once per call instead of once per pixel).
+constexpr int RS_MAXT = 6;
+struct ResTap {
+  int first;
+  float w[RS_MAXT];
+};
+
+__global__ void __launch_bounds__(256) resample_taps_kernel(ResTap *cols, ResTap *rows, int sw, int sh, int dw,
+                                                            int dh, int imode) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= dw + dh) return;
+  const bool is_col = i < dw;
+  const int o = is_col ? i : i - dw;
+  const float s = is_col ? (float)sw / (float)dw : (float)sh / (float)dh;
   const bool b5 = imode == 3, l3 = imode == 5;
-  float xb = b5 ? xm : xm - 0.5f, yb = b5 ? ym : ym - 0.5f;
-  xb = xb < 0.0f ? 0.0f : xb;
-  yb = yb < 0.0f ? 0.0f : yb;
-  const int xi = (int)xb, yi = (int)yb;
-  const float xf = xb - (float)xi, yf = yb - (float)yi;
-  const int n = l3 ? 6 : 4;
-  const int cx0 = l3 ? xi - 2 : xi - 1, cy0 = yi - 1;
-  const float tx = b5 ? xf + 1.0f : (l3 ? xf - 2.0f : xf - 1.0f);
-  const float ty = b5 ? yf + 1.0f : (l3 ? yf - 2.0f : yf - 1.0f);
-  auto w = [&](float d) { return b5 ? wt_b5(d) : (l3 ? wt_l3(d) : wt_cf(d)); };
-  float out = 0.0f;
-  for (int k = 0; k < n; ++k) {
-    const int y = min(max(cy0 + k, 0), sh - 1);
-    const float *row = reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + y * sp);
-    float acc = 0.0f;
-    for (int j = 0; j < n; ++j) {
-      const int x = min(max(cx0 + j, 0), sw - 1);
-      const int jw = (l3 && k == 1 && j == 4) ? 5 : j;
-      const float p = __fmul_rn(__ldg(row + x), w(b5 ? __fsub_rn(tx, (float)jw) : __fadd_rn(tx, (float)jw)));
-      acc = j == 0 ? p : __fadd_rn(acc, p);
-    }
-    const float q = __fmul_rn(acc, w(b5 ? __fsub_rn(ty, (float)k) : __fadd_rn(ty, (float)k)));
-    out = k == 0 ? q : __fadd_rn(out, q);
+  const float m = mapped(s, o);
+  float b = b5 ? m : m - 0.5f;
+  b = b < 0.0f ? 0.0f : b;
+  const int bi = (int)b;
+  const float f = b - (float)bi;
+  const float t = b5 ? f + 1.0f : (l3 ? f - 2.0f : f - 1.0f);
+  ResTap tap;
+  // columns x_int-2.. for L3, x_int-1.. otherwise; rows y_int-1.. for every mode
+  tap.first = (is_col && l3) ? bi - 2 : bi - 1;
+#pragma unroll
+  for (int j = 0; j < RS_MAXT; ++j) {
+    const float d = b5 ? __fsub_rn(t, (float)j) : __fadd_rn(t, (float)j);
+    tap.w[j] = b5 ? wt_b5(d) : (l3 ? wt_l3(d) : wt_cf(d));
   }
-  return out;
+  (is_col ? cols : rows)[o] = tap;
 }
 
+// out(x, y) = sum_k (sum_j src(x_j, y_k) w_j) w_k, every product and sum rounded
+// separately in the macros' order; taps clamped to the image.  The reference
+// gives the fifth tap of the second row of L3 the sixth tap's weight.
+template <int N, bool L3>
+__global__ void __launch_bounds__(256) resample_filtered_kernel(const char *in, int64_t ip, int64_t ibs, int sw,
+                                                                int sh, char *out, int64_t op, int64_t obs, int dw,
+                                                                int dh, const ResTap *cols, const ResTap *rows) {
+  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y, b = blockIdx.z;
+  if (x >= dw || y >= dh) return;
+  const float *src = reinterpret_cast<const float *>(in + (int64_t)b * ibs);
+  const ResTap cx = cols[x], cy = rows[y];
+  float acc_out = 0.0f;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    const int yy = min(max(cy.first + k, 0), sh - 1);
+    const float *row = reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + yy * ip);
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const int xx = min(max(cx.first + j, 0), sw - 1);
+      const float wj = (L3 && k == 1 && j == 4) ? cx.w[5] : cx.w[j];
+      const float p = __fmul_rn(__ldg(row + xx), wj);
+      acc = j == 0 ? p : __fadd_rn(acc, p);
+    }
+    const float q = __fmul_rn(acc, cy.w[k]);
+    acc_out = k == 0 ? q : __fadd_rn(acc_out, q);
+  }
+  reinterpret_cast<float *>(out + (int64_t)b * obs + (int64_t)y * op)[x] = acc_out;
+}
+
+// NN and LF: a thread per column and four rows 8 apart (a 32 x 32 block of
+// outputs per CTA), so that every thread has four independent reads in flight
+constexpr int RS_ROWS = 4;
 __global__ void __launch_bounds__(256) resample_kernel(const char *in, int64_t ip, int64_t ibs, int sw, int sh,
-                                                       char *out, int64_t op, int64_t obs, int dw, int dh, int batch,
-                                                       int imode) {
+                                                       char *out, int64_t op, int64_t obs, int dw, int dh, int imode) {
+  const int x = blockIdx.x * 32 + threadIdx.x, b = blockIdx.z;
+  if (x >= dw) return;
   const float sx = (float)sw / (float)dw, sy = (float)sh / (float)dh;
-  const int64_t n = (int64_t)dw * dh * batch;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const int x = (int)(i % dw);
-    const int64_t r = i / dw;
-    const int y = (int)(r % dh), b = (int)(r / dh);
-    const float *src = reinterpret_cast<const float *>(in + b * ibs);
-    float v;
+  const float *src = reinterpret_cast<const float *>(in + (int64_t)b * ibs);
+  float v[RS_ROWS];
+#pragma unroll
+  for (int k = 0; k < RS_ROWS; ++k) {
+    const int y = blockIdx.y * 8 * RS_ROWS + threadIdx.y + 8 * k;
+    if (y >= dh) break;
     if (imode == 1) {
       int xx = (int)mapped(sx, x), yy = (int)mapped(sy, y);
       xx = min(max(xx, 0), sw - 1);
       yy = min(max(yy, 0), sh - 1);
-      v = __ldg(reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + yy * ip) + xx);
-    } else if (imode == 2) {
-      v = lf_sample(src, ip, sw, sh, mapped(sx, x), mapped(sy, y));
+      v[k] = __ldg(reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + yy * ip) + xx);
     } else {
-      v = filtered_sample(src, ip, sw, sh, mapped(sx, x), mapped(sy, y), imode);
+      v[k] = lf_sample(src, ip, sw, sh, mapped(sx, x), mapped(sy, y));
     }
-    reinterpret_cast<float *>(out + b * obs + y * op)[x] = v;
+  }
+#pragma unroll
+  for (int k = 0; k < RS_ROWS; ++k) {
+    const int y = blockIdx.y * 8 * RS_ROWS + threadIdx.y + 8 * k;
+    if (y >= dh) break;
+    reinterpret_cast<float *>(out + (int64_t)b * obs + (int64_t)y * op)[x] = v[k];
   }
 }
 
@@ -496,11 +536,35 @@ extern "C" int hgb_resample(const hgb_view *in, const hgb_view *out, int imode, 
   HGB_REQUIRE(in->dtype == HGB_F32 && out->dtype == HGB_F32, "hgb_resample: f32 expected");
   HGB_REQUIRE(imode >= 1 && imode <= 5, "hgb_resample: imode must be 1 (NN), 2 (LF), 3 (B5), 4 (CF) or 5 (L3)");
   HGB_REQUIRE(in->batch == out->batch, "hgb_resample: batch mismatch");
+  HGB_REQUIRE(in->pitch % 4 == 0 && out->pitch % 4 == 0, "hgb_resample: pitches must be whole floats");
+  HGB_REQUIRE(out->batch <= 65535, "hgb_resample: at most 65535 images per call");
   cudaStream_t st = (cudaStream_t)stream;
-  const int64_t n = (int64_t)out->width * out->height * out->batch;
+  const dim3 grid(cdiv(out->width, 32), cdiv(out->height, 8), out->batch), block(32, 8);
+  if (imode <= 2) {
+    const dim3 g4(grid.x, cdiv(out->height, 8 * RS_ROWS), out->batch);
+    cudaEvent_t ev = before_launch(st);
+    resample_kernel<<<g4, block, 0, st>>>((const char *)in->data, in->pitch, in->batch_stride, in->width,
+                                            in->height, (char *)out->data, out->pitch, out->batch_stride,
+                                            out->width, out->height, imode);
+    return after_launch("resample_kernel", st, ev);
+  }
+  // filtered modes: tap tables in the library workspace (calls sharing it are ordered on one stream)
+  Workspace ws;
+  rc = workspace_get(((size_t)out->width + out->height) * sizeof(ResTap), &ws);
+  if (rc) return rc;
+  ResTap *cols = (ResTap *)ws.base, *rows = cols + out->width;
   cudaEvent_t ev = before_launch(st);
-  resample_kernel<<<grid_for(n, 256), 256, 0, st>>>((const char *)in->data, in->pitch, in->batch_stride, in->width,
-                                                    in->height, (char *)out->data, out->pitch, out->batch_stride,
-                                                    out->width, out->height, out->batch, imode);
-  return after_launch("resample_kernel", st, ev);
+  resample_taps_kernel<<<cdiv(out->width + out->height, 256), 256, 0, st>>>(cols, rows, in->width, in->height,
+                                                                             out->width, out->height, imode);
+  const char *src = (const char *)in->data;
+  char *dst = (char *)out->data;
+  if (imode == 5)
+    resample_filtered_kernel<6, true><<<grid, block, 0, st>>>(src, in->pitch, in->batch_stride, in->width,
+                                                              in->height, dst, out->pitch, out->batch_stride,
+                                                              out->width, out->height, cols, rows);
+  else
+    resample_filtered_kernel<4, false><<<grid, block, 0, st>>>(src, in->pitch, in->batch_stride, in->width,
+                                                               in->height, dst, out->pitch, out->batch_stride,
+                                                               out->width, out->height, cols, rows);
+  return after_launch("resample_filtered_kernel", st, ev);
 }

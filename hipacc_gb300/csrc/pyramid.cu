@@ -38,21 +38,36 @@
 #include <cstring>
 #include <vector>
 
+#include <cstdio>
+
+#include "autotune.h"
 #include "local_op.cuh"
 #include "tma.cuh"
 
 namespace hgb {
 namespace {
 
-constexpr int PY_TW = 64, PY_TH = 32;              // L_l tile
-constexpr int PY_GW = PY_TW / 2 + 2, PY_GH = PY_TH / 2 + 2;  // G_{l+1} tile + halo
-constexpr int PY_SW = PY_TW + 12, PY_SH = PY_TH + 12;        // staged G_l region bound
-// TMA box of the staged region: its x origin is rounded down to a multiple of
-// 4 floats (16 bytes), so the box is 4 floats wider than the region bound
-constexpr int PY_BW = PY_SW + 4, PY_BH = PY_SH;
-// 128 threads and ten CTAs per SM: more staged boxes in flight per SM (measured
-// 1.30 -> 1.01 ms per batch against 256 threads and five CTAs)
-constexpr int PY_THREADS = 128;
+// Tile configuration of the level-tile kernels: an L_l tile of TW x TH pixels,
+// NT threads.  The G_{l+1} tile with its halo is GW x GH; the staged G_l region
+// is bounded by SW x SH, and its TMA box is BW x BH (the x origin is rounded
+// down to a multiple of 4 floats, 16 bytes, so the box is 4 floats wider).
+template <int TW_, int TH_, int NT_>
+struct PyCfg {
+  static constexpr int TW = TW_, TH = TH_, NT = NT_;
+  static constexpr int GW = TW / 2 + 2, GH = TH / 2 + 2;
+  static constexpr int SW = TW + 12, SH = TH + 12;
+  static constexpr int BW = SW + 4, BH = SH;
+  static constexpr int MIN_CTAS = 1280 / NT;  // ten CTAs of 128 threads per SM
+};
+// configurations the autotuner chooses from (config 0 is the default; the
+// collapse uses its work-list).  64 x 32 at 128 threads and ten CTAs per SM
+// measured 1.30 -> 1.01 ms per batch against 256 threads and five CTAs.
+using PyCfg0 = PyCfg<64, 32, 128>;
+using PyCfg1 = PyCfg<64, 16, 128>;
+using PyCfg2 = PyCfg<32, 32, 128>;
+using PyCfg3 = PyCfg<64, 32, 256>;
+constexpr int kPyCfgs = 4;
+constexpr int PY_TW = 64, PY_TH = 32;  // config 0, the collapse's tiles
 
 struct LevelMeta {
   float *g;    // Gaussian level
@@ -72,7 +87,7 @@ struct __align__(16) PyrTile {
 
 struct PyrParams {
   const LevelMeta *meta;  // [img * levels + l]
-  const CUtensorMap *maps;  // [img * levels + l]: G_l tensor maps, box PY_BW x PY_BH
+  const CUtensorMap *maps;  // [img * levels + l]: G_l tensor maps, box BW x BH of the configuration
   const PyrTile *tiles;
   int ntiles;
   int levels;
@@ -82,6 +97,7 @@ struct PyrParams {
   unsigned int *abort;      // set when a tile failed: dependants stop waiting (persistent form)
   int *status;
   long long max_polls;      // limit of every bounded wait
+  int single;               // one tile per CTA (pyr_persistent_kernel)
   int inject_kind;          // wait test (hgb_pyramid_plan_wait_test): 0 none, 1 withhold, 2 no copy
   int inject_level;
   float mask[25];
@@ -141,13 +157,13 @@ __device__ __forceinline__ void load5(const float *row, float v[5]) {
 // 5x5 blur at two samples of one column whose top rows are D apart: rows
 // 0..D+4 of `src` are read once; each sample's 25 taps stay row-major fused
 // multiply-adds (the reference's order).
-template <int D, bool ODD>
+template <int D, bool ODD, int BW>
 __device__ __forceinline__ void blur_pair(const float *mask, const float *src, float &a0, float &a1) {
   float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
   for (int R = 0; R < D + 5; ++R) {
     float v[5];
-    load5<ODD>(src + R * PY_BW, v);
+    load5<ODD>(src + R * BW, v);
     if (R < 5) {
 #pragma unroll
       for (int mx = 0; mx < 5; ++mx) s0 = __fmaf_rn(mask[R * 5 + mx], v[mx], s0);
@@ -161,17 +177,19 @@ __device__ __forceinline__ void blur_pair(const float *mask, const float *src, f
   a1 = s1;
 }
 
+template <int BW>
 __device__ __forceinline__ float blur_one(const float *mask, const float *src) {
   float acc = 0.0f;
 #pragma unroll
   for (int my = 0; my < 5; ++my)
 #pragma unroll
-    for (int mx = 0; mx < 5; ++mx) acc = __fmaf_rn(mask[my * 5 + mx], src[my * PY_BW + mx], acc);
+    for (int mx = 0; mx < 5; ++mx) acc = __fmaf_rn(mask[my * 5 + mx], src[my * BW + mx], acc);
   return acc;
 }
 
-// One 64 x 32 tile of L_level (and the owned part of G_{level+1}).
+// One TW x TH tile of L_level (and the owned part of G_{level+1}).
 // `bar` is the CTA's mbarrier and `phase` its next phase parity.
+template <class C>
 __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, float *gt, LfTap *cols, LfTap *rows,
                          int *ncx, int *ncy, uint64_t *bar, unsigned &phase, bool coherent) {
   // ---- stage the G_l box [by, by + BH) x [bx, bx + BW) with one TMA load
@@ -180,7 +198,7 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
     // (generic stores, acquired by the level wait) and the previous tile's
     // patch wrote `stage` with generic stores: order both before the copy
     if (coherent) asm volatile("fence.proxy.async;" ::: "memory");
-    mbar_expect_tx(bar, PY_BW * PY_BH * 4);
+    mbar_expect_tx(bar, C::BW * C::BH * 4);
     // wait test kind 2: the bytes are expected but no copy is issued, so the
     // barrier's phase never completes (nothing is in flight when the wait expires)
     if (!(p.inject_kind == 2 && t.level == p.inject_level))
@@ -192,8 +210,8 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
   // nearest-neighbour scale G_l -> G_{l+1} and linear-filtering scale G_{l+1} -> L_l
   const float Sx = (float)wl / (float)wn, Sy = (float)hl / (float)hn;
   const float sx = (float)wn / (float)wl, sy = (float)hn / (float)hl;
-  const int gx0 = max(0, t.x0 / 2 - 1), gx1 = min(wn, t.x0 / 2 + PY_TW / 2 + 1);
-  const int gy0 = max(0, t.y0 / 2 - 1), gy1 = min(hn, t.y0 / 2 + PY_TH / 2 + 1);
+  const int gx0 = max(0, t.x0 / 2 - 1), gx1 = min(wn, t.x0 / 2 + C::TW / 2 + 1);
+  const int gy0 = max(0, t.y0 / 2 - 1), gy1 = min(hn, t.y0 / 2 + C::TH / 2 + 1);
   auto nn = [](float S, int x, int lim) {
     int v = (int)__fmaf_rn(S, (float)x, S * 0.5f);
     return v < lim ? v : lim - 1;
@@ -204,16 +222,16 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
   const int bx0 = rx0 & ~3, ox = rx0 - bx0;
   // while the box lands: the linear-filtering taps of the tile's columns and
   // rows, and the staged positions of the blur's nearest-neighbour samples
-  for (int i = threadIdx.x; i < PY_TW + PY_TH + PY_GW + PY_GH; i += PY_THREADS) {
-    if (i < PY_TW) {
+  for (int i = threadIdx.x; i < C::TW + C::TH + C::GW + C::GH; i += C::NT) {
+    if (i < C::TW) {
       cols[i] = lf_tap(sx, t.x0 + i, wn, gx0);
-    } else if (i < PY_TW + PY_TH) {
-      rows[i - PY_TW] = lf_tap(sy, t.y0 + i - PY_TW, hn, gy0);
-    } else if (i < PY_TW + PY_TH + PY_GW) {
-      const int q = i - PY_TW - PY_TH;
+    } else if (i < C::TW + C::TH) {
+      rows[i - C::TW] = lf_tap(sy, t.y0 + i - C::TW, hn, gy0);
+    } else if (i < C::TW + C::TH + C::GW) {
+      const int q = i - C::TW - C::TH;
       ncx[q] = nn(Sx, gx0 + q, wl) - 2 - rx0 + ox;
     } else {
-      const int r = i - PY_TW - PY_TH - PY_GW;
+      const int r = i - C::TW - C::TH - C::GW;
       ncy[r] = nn(Sy, gy0 + r, hl) - 2 - ry0;
     }
   }
@@ -230,16 +248,16 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
     if (threadIdx.x == 0) record_status(p.status, HGB_ERR_INTERNAL);
     return false;
   }
-  if (bx0 < 0 || bx0 + PY_BW > wl || ry0 < 0 || ry0 + PY_BH > hl) {
+  if (bx0 < 0 || bx0 + C::BW > wl || ry0 < 0 || ry0 + C::BH > hl) {
     // box cells outside the level (zero-filled by TMA) through the boundary
     // remap: left / right columns, top / bottom rows.  The tile reads at most
     // two columns (rows) past the level's last one (the blur's reach from the
     // last nearest-neighbour position w_l - 1), so the patch stops there.
-    const int cw = min(PY_BW, wl + 2 - bx0), ch = min(PY_BH, hl + 2 - ry0);  // box part the tile reads
+    const int cw = min(C::BW, wl + 2 - bx0), ch = min(C::BH, hl + 2 - ry0);  // box part the tile reads
     const int nl = max(0, min(cw, -bx0)), rs = max(0, min(cw, wl - bx0));
     const int nt = max(0, min(ch, -ry0)), bs = max(0, min(ch, hl - ry0));
     const int ncl = nl * ch, ncr = (cw - rs) * ch, nrt = nt * cw, nrb = (ch - bs) * cw;
-    for (int c = threadIdx.x; c < ncl + ncr + nrt + nrb; c += PY_THREADS) {
+    for (int c = threadIdx.x; c < ncl + ncr + nrt + nrb; c += C::NT) {
       int r, q;
       if (c < ncl) {
         r = c / nl;
@@ -259,7 +277,7 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
         q = d - rr * cw;
       }
       const int yy = remap(p.bmode, ry0 + r, 0, hl), xx = remap(p.bmode, bx0 + q, 0, wl);
-      stage[r * PY_BW + q] = (yy == (int)0x80000000 || xx == (int)0x80000000)
+      stage[r * C::BW + q] = (yy == (int)0x80000000 || xx == (int)0x80000000)
                                  ? 0.0f
                                  : ld_level(A.g + (int64_t)yy * A.pitch + xx, coherent);
     }
@@ -271,14 +289,14 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
   const int gw = gx1 - gx0, gh = gy1 - gy0;
   const int ownx0 = t.x0 / 2, owny0 = t.y0 / 2;
   auto put = [&](int q, int r, float v) {
-    gt[r * PY_GW + q] = v;
+    gt[r * C::GW + q] = v;
     // owned pixels of G_{l+1}: x' in [x0/2, x0/2 + TW/2), y' likewise
     const int xp = gx0 + q, yp = gy0 + r;
-    if (xp >= ownx0 && xp < ownx0 + PY_TW / 2 && yp >= owny0 && yp < owny0 + PY_TH / 2)
+    if (xp >= ownx0 && xp < ownx0 + C::TW / 2 && yp >= owny0 && yp < owny0 + C::TH / 2)
       __stwb(B.g + (int64_t)yp * B.pitch + xp, v);
   };
-  for (int c = threadIdx.x; c < PY_GW * (PY_GH / 2); c += PY_THREADS) {
-    const int r2 = c / PY_GW, q = c - r2 * PY_GW;  // constant divisor
+  for (int c = threadIdx.x; c < C::GW * (C::GH / 2); c += C::NT) {
+    const int r2 = c / C::GW, q = c - r2 * C::GW;  // constant divisor
     const int r = 2 * r2;
     if (q >= gw || r >= gh) continue;
     const int cx = ncx[q];
@@ -286,15 +304,15 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
     const int cy0 = cy.x;
     const bool two = r + 1 < gh;
     const int d = two ? cy.y - cy0 : 0;
-    const float *src = stage + cy0 * PY_BW + cx;
+    const float *src = stage + cy0 * C::BW + cx;
     float a0, a1 = 0.0f;
     if (d == 2) {
-      if (cx & 1) blur_pair<2, true>(p.mask, src, a0, a1); else blur_pair<2, false>(p.mask, src, a0, a1);
+      if (cx & 1) blur_pair<2, true, C::BW>(p.mask, src, a0, a1); else blur_pair<2, false, C::BW>(p.mask, src, a0, a1);
     } else if (d == 3) {
-      if (cx & 1) blur_pair<3, true>(p.mask, src, a0, a1); else blur_pair<3, false>(p.mask, src, a0, a1);
+      if (cx & 1) blur_pair<3, true, C::BW>(p.mask, src, a0, a1); else blur_pair<3, false, C::BW>(p.mask, src, a0, a1);
     } else {
-      a0 = blur_one(p.mask, src);
-      if (two) a1 = blur_one(p.mask, src + d * PY_BW);
+      a0 = blur_one<C::BW>(p.mask, src);
+      if (two) a1 = blur_one<C::BW>(p.mask, src + d * C::BW);
     }
     put(q, r, a0);
     if (two) put(q, r + 1, a1);
@@ -302,7 +320,7 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
   __syncthreads();
   // ---- L_l = G_l - LF(G_{l+1}): a thread per pair of columns, rows strided;
   // the two columns' arithmetic as packed FP32 (per-lane rounding unchanged)
-  const int tx = threadIdx.x % (PY_TW / 2);
+  const int tx = threadIdx.x % (C::TW / 2);
   const int x = t.x0 + 2 * tx;
   if (x < wl) {
     const LfTap c0 = cols[2 * tx], c1 = cols[2 * tx + 1];
@@ -310,18 +328,18 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
     const float *gcol = stage + (x - rx0 + ox);  // even: x and bx0 are even
     const bool pair = x + 1 < wl;
 #pragma unroll 1
-    for (int r = threadIdx.x / (PY_TW / 2); r < PY_TH; r += PY_THREADS / (PY_TW / 2)) {
+    for (int r = threadIdx.x / (C::TW / 2); r < C::TH; r += C::NT / (C::TW / 2)) {
       const int y = t.y0 + r;
       if (y >= hl) break;
       const LfTap cy = rows[r];
       const f2 yg = f2_pack(cy.g, cy.g), yf = f2_pack(cy.f, cy.f);
       const f2 wa = f2_mul(cg, yg), wb = f2_mul(cf, yg), wc = f2_mul(cg, yf), wd = f2_mul(cf, yf);
-      const float *ga = gt + cy.a * PY_GW, *gc = gt + cy.c * PY_GW;
+      const float *ga = gt + cy.a * C::GW, *gc = gt + cy.c * C::GW;
       f2 lf = f2_mul(wa, f2_pack(ga[c0.a], ga[c1.a]));
       lf = f2_fma(wb, f2_pack(ga[c0.c], ga[c1.c]), lf);
       lf = f2_fma(wc, f2_pack(gc[c0.a], gc[c1.a]), lf);
       lf = f2_fma(wd, f2_pack(gc[c0.c], gc[c1.c]), lf);
-      const float2 g = *reinterpret_cast<const float2 *>(gcol + (y - ry0) * PY_BW);
+      const float2 g = *reinterpret_cast<const float2 *>(gcol + (y - ry0) * C::BW);
       const f2 v = f2_sub(f2_pack(g.x, g.y), lf);
       float *dst = A.lap + (int64_t)y * A.pitch + x;
       if (pair)
@@ -333,11 +351,12 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
   return true;
 }
 
-__global__ void __launch_bounds__(PY_THREADS, 10) pyr_level_kernel(const __grid_constant__ PyrParams p, int first) {
-  __shared__ __align__(128) float stage[PY_BW * PY_BH];
-  __shared__ float gt[PY_GW * PY_GH];
-  __shared__ LfTap cols[PY_TW], rows[PY_TH];
-  __shared__ __align__(8) int ncx[PY_GW], ncy[PY_GH];
+template <class C>
+__global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_level_kernel(const __grid_constant__ PyrParams p, int first) {
+  __shared__ __align__(128) float stage[C::BW * C::BH];
+  __shared__ float gt[C::GW * C::GH];
+  __shared__ LfTap cols[C::TW], rows[C::TH];
+  __shared__ __align__(8) int ncx[C::GW], ncy[C::GH];
   __shared__ __align__(8) uint64_t bar;
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
@@ -345,14 +364,20 @@ __global__ void __launch_bounds__(PY_THREADS, 10) pyr_level_kernel(const __grid_
   }
   __syncthreads();
   unsigned phase = 0;
-  pyr_tile(p, p.tiles[first + blockIdx.x], stage, gt, cols, rows, ncx, ncy, &bar, phase, false);
+  pyr_tile<C>(p, p.tiles[first + blockIdx.x], stage, gt, cols, rows, ncx, ncy, &bar, phase, false);
 }
 
-__global__ void __launch_bounds__(PY_THREADS, 10) pyr_persistent_kernel(const __grid_constant__ PyrParams p) {
-  __shared__ __align__(128) float stage[PY_BW * PY_BH];
-  __shared__ float gt[PY_GW * PY_GH];
-  __shared__ LfTap cols[PY_TW], rows[PY_TH];
-  __shared__ __align__(8) int ncx[PY_GW], ncy[PY_GH];
+// One launch over the whole work-list.  p.single = 0: persistent CTAs (one
+// wave) claim tiles until the list ends; p.single = 1: a CTA per tile, each
+// claiming one tile when the hardware starts it.  Either way a tile only waits
+// on tiles claimed before it, so the claimers of what it waits for are running
+// or done.
+template <class C>
+__global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(const __grid_constant__ PyrParams p) {
+  __shared__ __align__(128) float stage[C::BW * C::BH];
+  __shared__ float gt[C::GW * C::GH];
+  __shared__ LfTap cols[C::TW], rows[C::TH];
+  __shared__ __align__(8) int ncx[C::GW], ncy[C::GH];
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_t;
   __shared__ int s_ok;
@@ -398,15 +423,17 @@ __global__ void __launch_bounds__(PY_THREADS, 10) pyr_persistent_kernel(const __
     if (t >= p.ntiles || s_ok == 0) return;
     const PyrTile tl = p.tiles[t];
     if (s_ok == 2) {  // uniform: every thread read s_ok after the barrier
+      if (p.single) return;
       __syncthreads();  // s_t / s_ok are read before thread 0 claims again
       continue;
     }
-    if (!pyr_tile(p, tl, stage, gt, cols, rows, ncx, ncy, &bar, phase, true)) {
+    if (!pyr_tile<C>(p, tl, stage, gt, cols, rows, ncx, ncy, &bar, phase, true)) {
       if (threadIdx.x == 0) atomicExch(p.abort, 1u);
       return;
     }
     __syncthreads();
     if (threadIdx.x == 0) red_release_add(&p.done[tl.img * p.levels + tl.level], 1u);
+    if (p.single) return;
   }
 }
 
@@ -462,25 +489,98 @@ __global__ void __launch_bounds__(256) pyr_restore_kernel(const __grid_constant_
 
 using namespace hgb;
 
+// Work-list, tensor maps and tile counts of one tile configuration
+struct PyrConfigData {
+  std::vector<int> level_first;    // first tile of each level in the list
+  std::vector<int> level_count;
+  CUtensorMap *d_maps = nullptr;   // G_l tensor maps, [img * levels + l]
+  PyrTile *d_tiles = nullptr;
+  int *d_ntiles = nullptr;         // tiles of level l of image i, [img * levels + l]
+  int ntiles = 0;
+  int persistent_ctas = 0;
+};
+
 struct hgb_pyramid_plan {
   int n = 0, levels = 0, bmode = 0;
   float mask[25];
   std::vector<int> w0, h0;
   std::vector<LevelMeta> meta;     // host copy
-  std::vector<int> level_first;    // first tile of each level in the list
-  std::vector<int> level_count;
   void *arena = nullptr;           // all levels of all images
   void *tmp = nullptr;             // blur buffer of the reference launch structure
   LevelMeta *d_meta = nullptr;
-  CUtensorMap *d_maps = nullptr;   // G_l tensor maps, [img * levels + l]
-  PyrTile *d_tiles = nullptr;
-  int *d_ntiles = nullptr;
   unsigned int *d_ctrl = nullptr;  // done counters [n*levels] + claim counter + abort flag
-  int ntiles = 0;
-  int persistent_ctas = 0;
+  PyrConfigData cfg[kPyCfgs];
   long long max_polls = kMaxSpins;
   int inject_kind = 0, inject_level = 0;
 };
+
+namespace {
+
+template <class C>
+int build_config(hgb_pyramid_plan *P, int c) {
+  PyrConfigData &D = P->cfg[c];
+  const int n = P->n, levels = P->levels;
+  // work-list: levels ascending, then images, then tiles row-major
+  std::vector<PyrTile> tiles;
+  std::vector<int> nil((size_t)n * levels, 0);
+  for (int l = 0; l + 1 < levels; ++l) {
+    D.level_first.push_back((int)tiles.size());
+    for (int i = 0; i < n; ++i) {
+      const LevelMeta &m = P->meta[(size_t)i * levels + l];
+      const LevelMeta &mn = P->meta[(size_t)i * levels + l + 1];
+      const float Sx = (float)m.w / (float)mn.w, Sy = (float)m.h / (float)mn.h;
+      auto nn = [](float S, int v, int lim) {
+        const int r = (int)std::fmaf(S, (float)v, S * 0.5f);
+        return r < lim ? r : lim - 1;
+      };
+      for (int y = 0; y < m.h; y += C::TH)
+        for (int x = 0; x < m.w; x += C::TW) {
+          // the kernel's box origin, with the same single-precision arithmetic
+          const int rx0 = nn(Sx, std::max(0, x / 2 - 1), m.w) - 2, ry0 = nn(Sy, std::max(0, y / 2 - 1), m.h) - 2;
+          tiles.push_back(PyrTile{i, l, x, y, rx0 & ~3, ry0, 0, 0});
+        }
+      nil[(size_t)i * levels + l] = cdiv(m.w, C::TW) * cdiv(m.h, C::TH);
+    }
+    D.level_count.push_back((int)tiles.size() - D.level_first.back());
+  }
+  D.ntiles = (int)tiles.size();
+  // tensor maps of every Gaussian level a tile stages
+  std::vector<CUtensorMap> maps(P->meta.size());
+  memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+  for (size_t k = 0; k < P->meta.size(); ++k) {
+    if ((int)(k % levels) + 1 >= levels) continue;
+    const LevelMeta &m = P->meta[k];
+    const int rc = make_tensor_map_3d(&maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, m.g, m.w, m.h, 1,
+                                      (int64_t)m.pitch * 4, (int64_t)m.pitch * 4 * m.h, C::BW, C::BH);
+    if (rc != HGB_OK) return rc;
+  }
+  cudaError_t e = cudaMalloc((void **)&D.d_tiles, tiles.size() * sizeof(PyrTile));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&D.d_ntiles, nil.size() * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&D.d_maps, maps.size() * sizeof(CUtensorMap));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(D.d_tiles, tiles.data(), tiles.size() * sizeof(PyrTile), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(D.d_ntiles, nil.data(), nil.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(D.d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_error(e, "hgb_pyramid_plan_create: work-list upload");
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pyr_persistent_kernel<C>, C::NT, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  D.persistent_ctas = num_sms() * per_sm;
+  return HGB_OK;
+}
+
+void free_config(PyrConfigData &D) {
+  cudaFree(D.d_maps);
+  cudaFree(D.d_tiles);
+  cudaFree(D.d_ntiles);
+  D.d_maps = nullptr;
+  D.d_tiles = nullptr;
+  D.d_ntiles = nullptr;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -519,37 +619,11 @@ int hgb_pyramid_plan_create(int n_images, const int *widths, const int *heights,
       h /= 2;
     }
   }
-  // work-list: levels ascending, then images, then tiles row-major
-  std::vector<PyrTile> tiles;
-  std::vector<int> nil((size_t)n_images * levels, 0);
-  for (int l = 0; l + 1 < levels; ++l) {
-    P->level_first.push_back((int)tiles.size());
-    for (int i = 0; i < n_images; ++i) {
-      const LevelMeta &m = P->meta[(size_t)i * levels + l];
-      for (int y = 0; y < m.h; y += PY_TH)
-        for (int x = 0; x < m.w; x += PY_TW) {
-          // the kernel's box origin, with the same single-precision arithmetic
-          const LevelMeta &mn = P->meta[(size_t)i * levels + l + 1];
-          const float Sx = (float)m.w / (float)mn.w, Sy = (float)m.h / (float)mn.h;
-          auto nn = [](float S, int v, int lim) {
-            const int r = (int)std::fmaf(S, (float)v, S * 0.5f);
-            return r < lim ? r : lim - 1;
-          };
-          const int rx0 = nn(Sx, std::max(0, x / 2 - 1), m.w) - 2, ry0 = nn(Sy, std::max(0, y / 2 - 1), m.h) - 2;
-          tiles.push_back(PyrTile{i, l, x, y, rx0 & ~3, ry0, 0, 0});
-        }
-      nil[(size_t)i * levels + l] = cdiv(m.w, PY_TW) * cdiv(m.h, PY_TH);
-    }
-    P->level_count.push_back((int)tiles.size() - P->level_first.back());
-  }
-  P->ntiles = (int)tiles.size();
   cudaError_t e = cudaMalloc(&P->arena, bytes);
   if (e == cudaSuccess) e = cudaMemset(P->arena, 0, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&P->tmp, tmp_bytes);
   if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_meta, P->meta.size() * sizeof(LevelMeta));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_tiles, tiles.size() * sizeof(PyrTile));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_ntiles, nil.size() * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_ctrl, (nil.size() + 2) * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&P->d_ctrl, ((size_t)n_images * levels + 2) * sizeof(unsigned int));
   if (e != cudaSuccess) {
     hgb_pyramid_plan_destroy(P);
     return cuda_error(e, "hgb_pyramid_plan_create: allocation");
@@ -558,36 +632,19 @@ int hgb_pyramid_plan_create(int n_images, const int *widths, const int *heights,
     P->meta[k].g = (float *)((char *)P->arena + goff[k]);
     P->meta[k].lap = ((int)(k % levels) + 1 < levels) ? (float *)((char *)P->arena + loff[k]) : nullptr;
   }
-  // tensor maps of every Gaussian level a tile stages (box PY_BW x PY_BH)
-  std::vector<CUtensorMap> maps(P->meta.size());
-  memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
-  for (size_t k = 0; k < P->meta.size(); ++k) {
-    if ((int)(k % levels) + 1 >= levels) continue;
-    const LevelMeta &m = P->meta[k];
-    const int rc = make_tensor_map_3d(&maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, m.g, m.w, m.h, 1,
-                                      (int64_t)m.pitch * 4, (int64_t)m.pitch * 4 * m.h, PY_BW, PY_BH);
-    if (rc != HGB_OK) {
-      hgb_pyramid_plan_destroy(P);
-      return rc;
-    }
-  }
-  e = cudaMalloc((void **)&P->d_maps, maps.size() * sizeof(CUtensorMap));
-  if (e == cudaSuccess)
-    e = cudaMemcpy(P->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(P->d_meta, P->meta.data(), P->meta.size() * sizeof(LevelMeta), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(P->d_tiles, tiles.data(), tiles.size() * sizeof(PyrTile), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(P->d_ntiles, nil.data(), nil.size() * sizeof(int), cudaMemcpyHostToDevice);
+  e = cudaMemcpy(P->d_meta, P->meta.data(), P->meta.size() * sizeof(LevelMeta), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     hgb_pyramid_plan_destroy(P);
     return cuda_error(e, "hgb_pyramid_plan_create: upload");
   }
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pyr_persistent_kernel, PY_THREADS, 0) != cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
-  P->persistent_ctas = num_sms() * per_sm;
+  int rc = build_config<PyCfg0>(P, 0);
+  if (rc == HGB_OK) rc = build_config<PyCfg1>(P, 1);
+  if (rc == HGB_OK) rc = build_config<PyCfg2>(P, 2);
+  if (rc == HGB_OK) rc = build_config<PyCfg3>(P, 3);
+  if (rc != HGB_OK) {
+    hgb_pyramid_plan_destroy(P);
+    return rc;
+  }
   *out = P;
   return HGB_OK;
 }
@@ -597,10 +654,8 @@ int hgb_pyramid_plan_destroy(hgb_pyramid_plan *P) {
   cudaFree(P->arena);
   cudaFree(P->tmp);
   cudaFree(P->d_meta);
-  cudaFree(P->d_maps);
-  cudaFree(P->d_tiles);
-  cudaFree(P->d_ntiles);
   cudaFree(P->d_ctrl);
+  for (int c = 0; c < kPyCfgs; ++c) free_config(P->cfg[c]);
   delete P;
   return HGB_OK;
 }
@@ -627,15 +682,16 @@ int hgb_pyramid_level_view(const hgb_pyramid_plan *P, int image, int level, hgb_
   return HGB_OK;
 }
 
-static void fill_params(const hgb_pyramid_plan *P, PyrParams *p) {
+static void fill_params(const hgb_pyramid_plan *P, int c, PyrParams *p) {
   memset(p, 0, sizeof(*p));
+  const PyrConfigData &D = P->cfg[c];
   p->meta = P->d_meta;
-  p->maps = P->d_maps;
-  p->tiles = P->d_tiles;
-  p->ntiles = P->ntiles;
+  p->maps = D.d_maps;
+  p->tiles = D.d_tiles;
+  p->ntiles = D.ntiles;
   p->levels = P->levels;
   p->done = P->d_ctrl;
-  p->ntiles_il = P->d_ntiles;
+  p->ntiles_il = D.d_ntiles;
   p->work = P->d_ctrl + (size_t)P->n * P->levels;
   p->abort = p->work + 1;
   p->status = device_status_word();
@@ -646,28 +702,61 @@ static void fill_params(const hgb_pyramid_plan *P, PyrParams *p) {
   p->bmode = P->bmode;
 }
 
+}  // extern "C"
+
+template <class C>
+static int launch_decompose(const hgb_pyramid_plan *P, int c, int mode, int single, cudaStream_t st) {
+  const PyrConfigData &D = P->cfg[c];
+  PyrParams p;
+  fill_params(P, c, &p);
+  if (mode == 0) {
+    HGB_CHECK_CUDA(cudaMemsetAsync(P->d_ctrl, 0, ((size_t)P->n * P->levels + 2) * sizeof(unsigned int), st));
+    p.single = single;
+    const int grid = single ? D.ntiles : std::min(D.persistent_ctas, D.ntiles);
+    cudaEvent_t ev = before_launch(st);
+    pyr_persistent_kernel<C><<<grid, C::NT, 0, st>>>(p);
+    return after_launch("pyr_persistent_kernel", st, ev);
+  }
+  for (int l = 0; l + 1 < P->levels; ++l) {
+    cudaEvent_t ev = before_launch(st);
+    pyr_level_kernel<C><<<D.level_count[l], C::NT, 0, st>>>(p, D.level_first[l]);
+    const int rc = after_launch("pyr_level_kernel", st, ev);
+    if (rc) return rc;
+  }
+  return HGB_OK;
+}
+
+static int launch_cfg(const hgb_pyramid_plan *P, int c, int mode, int single, cudaStream_t st) {
+  switch (c) {
+    case 1: return launch_decompose<PyCfg1>(P, c, mode, single, st);
+    case 2: return launch_decompose<PyCfg2>(P, c, mode, single, st);
+    case 3: return launch_decompose<PyCfg3>(P, c, mode, single, st);
+    default: return launch_decompose<PyCfg0>(P, c, mode, single, st);
+  }
+}
+
+extern "C" {
+
 int hgb_pyramid_decompose(hgb_pyramid_plan *P, int mode, void *stream) {
   HGB_REQUIRE(P, "hgb_pyramid_decompose: null plan");
   HGB_REQUIRE(mode >= 0 && mode <= 2, "hgb_pyramid_decompose: mode must be 0, 1 or 2");
   cudaStream_t st = (cudaStream_t)stream;
+  if (mode == 0 || mode == 1) {
+    // tile configuration (tile shape, threads) and, for the single launch,
+    // persistent CTAs or one CTA per tile: autotuned per batch shape
+    int64_t px = 0;
+    for (int i = 0; i < P->n; ++i) px += (int64_t)P->w0[i] * P->h0[i];
+    int lg = 0;
+    while ((int64_t(1) << lg) < px) ++lg;
+    char key[96];
+    snprintf(key, sizeof(key), "pyramid:m%d:n%d:l%d:px2^%d", mode, P->n, P->levels, lg);
+    const int ncfg = mode == 0 ? 2 * kPyCfgs : kPyCfgs;
+    return autotune_run(key, ncfg, st, [&](int k) {
+      return launch_cfg(P, k % kPyCfgs, mode, mode == 0 ? k / kPyCfgs : 0, st);
+    });
+  }
   PyrParams p;
-  fill_params(P, &p);
-  if (mode == 0) {
-    HGB_CHECK_CUDA(cudaMemsetAsync(P->d_ctrl, 0, ((size_t)P->n * P->levels + 2) * sizeof(unsigned int), st));
-    const int grid = std::min(P->persistent_ctas, P->ntiles);
-    cudaEvent_t ev = before_launch(st);
-    pyr_persistent_kernel<<<grid, PY_THREADS, 0, st>>>(p);
-    return after_launch("pyr_persistent_kernel", st, ev);
-  }
-  if (mode == 1) {
-    for (int l = 0; l + 1 < P->levels; ++l) {
-      cudaEvent_t ev = before_launch(st);
-      pyr_level_kernel<<<P->level_count[l], PY_THREADS, 0, st>>>(p, P->level_first[l]);
-      const int rc = after_launch("pyr_level_kernel", st, ev);
-      if (rc) return rc;
-    }
-    return HGB_OK;
-  }
+  fill_params(P, 0, &p);
   // mode 2: the reference's kernels, per image and level
   for (int i = 0; i < P->n; ++i) {
     for (int l = 0; l + 1 < P->levels; ++l) {
@@ -705,10 +794,10 @@ int hgb_pyramid_collapse(hgb_pyramid_plan *P, void *stream) {
   HGB_REQUIRE(P, "hgb_pyramid_collapse: null plan");
   cudaStream_t st = (cudaStream_t)stream;
   PyrParams p;
-  fill_params(P, &p);
+  fill_params(P, 0, &p);
   for (int l = P->levels - 2; l >= 0; --l) {
     cudaEvent_t ev = before_launch(st);
-    pyr_restore_kernel<<<P->level_count[l], 256, 0, st>>>(p, P->level_first[l]);
+    pyr_restore_kernel<<<P->cfg[0].level_count[l], 256, 0, st>>>(p, P->cfg[0].level_first[l]);
     const int rc = after_launch("pyr_restore_kernel", st, ev);
     if (rc) return rc;
   }

@@ -155,29 +155,101 @@ __device__ __forceinline__ typename Red<T, OP>::A block_fold(typename Red<T, OP>
   return a;  // valid in thread 0
 }
 
+// fold one 16-byte chunk (V elements, the last chunk of a row may be partial)
+template <typename T, int OP>
+__device__ __forceinline__ typename Red<T, OP>::A fold_chunk(typename Red<T, OP>::A acc, const uint4 &v, int valid) {
+  constexpr int V = 16 / sizeof(T);
+  const T *e = reinterpret_cast<const T *>(&v);
+#pragma unroll
+  for (int q = 0; q < V; ++q)
+    if (q < valid) acc = fold_value<T, OP>(acc, e[q]);
+  return acc;
+}
+
+// u8 sums: four bytes per dp4a into a 32-bit partial (at most 2^24 chunks of
+// 16 bytes per partial before it is folded into the 64-bit accumulator)
+__device__ __forceinline__ uint32_t byte_sum16(const uint4 &v, uint32_t s) {
+  s = __dp4a(v.x, 0x01010101u, s);
+  s = __dp4a(v.y, 0x01010101u, s);
+  s = __dp4a(v.z, 0x01010101u, s);
+  return __dp4a(v.w, 0x01010101u, s);
+}
+
 template <typename T, int OP>
 __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ RedParams p) {
   using R = Red<T, OP>;
   using A = typename R::A;
   constexpr int V = 16 / sizeof(T);
+  constexpr bool kByteSum = std::is_same<T, uint8_t>::value && OP == HGB_REDUCE_SUM;
+  constexpr int U = 4;  // chunks in flight per thread
   A acc = R::identity();
-  const int64_t items = (int64_t)p.batch * p.h * p.chunks_per_row;
+  uint32_t bsum = 0;
+  int bsum_n = 0;
+  const int cpr = p.chunks_per_row;
+  const int64_t items = (int64_t)p.batch * p.h * cpr;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < items; it += stride) {
-    const int chunk = (int)(it % p.chunks_per_row);
-    const int64_t rg = it / p.chunks_per_row;
-    const int b = (int)(rg / p.h), y = (int)(rg - (int64_t)b * p.h);
-    const T *row = reinterpret_cast<const T *>(p.in + b * p.bstride + (int64_t)(p.oy + y) * p.pitch) + p.ox;
-    const int x0 = chunk * V;
-    if (p.vec && x0 + V <= p.w) {
-      const uint4 v = ldg16(row + x0);
-      const T *e = reinterpret_cast<const T *>(&v);
+  // chunk position as (row of the batch, chunk of the row), advanced by the
+  // grid stride without a division per chunk
+  const int s_c = (int)(stride % cpr);
+  const int64_t s_r = stride / cpr;
+  const int s_ry = (int)(s_r % p.h), s_rb = (int)(s_r / p.h);  // the row stride as (images, rows)
+  int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int c = (int)(it % cpr);
+  int64_t rg = it / cpr;
+  int b = (int)(rg / p.h), y = (int)(rg - (int64_t)b * p.h);
+  auto advance = [&]() {
+    it += stride;
+    c += s_c;
+    y += s_ry;
+    b += s_rb;
+    if (c >= cpr) {
+      c -= cpr;
+      ++y;
+    }
+    if (y >= p.h) {  // y < 2h here: one wrap at most
+      y -= p.h;
+      ++b;
+    }
+  };
+  while (it < items) {
+    uint4 v[U];
+    int valid[U];
+    int n = 0;
 #pragma unroll
-      for (int q = 0; q < V; ++q) acc = fold_value<T, OP>(acc, e[q]);
-    } else {
-      for (int q = 0; q < V && x0 + q < p.w; ++q) acc = fold_value<T, OP>(acc, row[x0 + q]);
+    for (int u = 0; u < U; ++u) {
+      if (it < items) {
+        const T *row = reinterpret_cast<const T *>(p.in + b * p.bstride + (int64_t)(p.oy + y) * p.pitch) + p.ox;
+        const int x0 = c * V;
+        valid[u] = min(V, p.w - x0);
+        if (p.vec && valid[u] == V) {
+          v[u] = ldg16(row + x0);
+        } else {
+          T tmp[V];
+#pragma unroll
+          for (int q = 0; q < V; ++q) tmp[q] = q < valid[u] ? row[x0 + q] : T(0);
+          memcpy(&v[u], tmp, 16);
+        }
+        ++n;
+        advance();
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (u < n) {
+        if constexpr (kByteSum) {
+          bsum = byte_sum16(v[u], bsum);  // padding bytes of a partial chunk are zero
+          if (++bsum_n == (1 << 24)) {
+            acc = R::fold(acc, (A)bsum);
+            bsum = 0;
+            bsum_n = 0;
+          }
+        } else {
+          acc = fold_chunk<T, OP>(acc, v[u], valid[u]);
+        }
+      }
     }
   }
+  if constexpr (kByteSum) acc = R::fold(acc, (A)bsum);
   acc = block_fold<T, OP>(acc);
   if constexpr (std::is_integral<T>::value && OP != HGB_REDUCE_PROD) {
     // integers: order-preserving 64-bit keys folded with relaxed atomics,

@@ -57,3 +57,26 @@ def test_local_adjoint_is_transpose(gpu, oracle):
         lhs = float((y.double() * gt.double()).sum())
         rhs = float((xt.double() * gi.double()).sum())
         assert abs(lhs - rhs) <= 1e-4 * abs(lhs), (mode, lhs, rhs)
+
+
+@pytest.mark.parametrize("k", [3, 5, 7])
+@pytest.mark.parametrize("mode", [1, 2, 3, 4])
+def test_local_adjoint_mask_gradient_batch(gpu, oracle, k, mode):
+    """The mask gradient of a batch over many tiles (ragged edges): the sum over
+    every image of the batch, deterministic from run to run."""
+    rng = np.random.default_rng(hash(("b", k, mode)) % 2**32)
+    B, h, w = 2, 130, 211
+    img = rng.random((B, h, w)).astype(np.float32)
+    gout = rng.normal(0, 1, (B, h, w)).astype(np.float32)
+    mask = rng.normal(0, 1, (k, k)).astype(np.float32)
+    gi, gm = gpu.local_op_adjoint(torch.from_numpy(gout).cuda(), mask, mode, inp=torch.from_numpy(img).cuda())
+    _, gm2 = gpu.local_op_adjoint(torch.from_numpy(gout).cuda(), mask, mode, inp=torch.from_numpy(img).cuda())
+    torch.cuda.synchronize()
+    rgm = np.zeros((k, k))
+    for b in range(B):
+        rgi, g1 = scatter_adjoint(oracle, img[b].astype(np.float64), gout[b].astype(np.float64),
+                                  mask.astype(np.float64), mode)
+        rgm += g1
+        assert np.max(np.abs(gi[b].cpu().numpy() - rgi)) <= 1e-4 * max(1.0, np.max(np.abs(rgi)))
+    assert np.max(np.abs(gm.cpu().numpy() - rgm)) <= 1e-4 * max(1.0, np.max(np.abs(rgm)))
+    assert torch.equal(gm, gm2)

@@ -176,3 +176,67 @@ def test_pyramid_wait_test_arguments(gpu, oracle):
     assert lib.hgb_pyramid_plan_wait_test(plan._h, 10, 1, 2) == L.ERR_INVALID  # the last level has no tiles
     assert lib.hgb_pyramid_plan_wait_test(None, 10, 1, 0) == L.ERR_INVALID
     plan.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_pyramid_every_tile_configuration(gpu, oracle, mode, tmp_path):
+    """Every configuration the autotuner can choose for the fused launches
+    (tile shape and threads; for the single launch also persistent CTAs or one
+    CTA per tile), forced through a loaded choice file, is bit-exact."""
+    import json
+    import math
+
+    from hipacc_gb300 import _lib as L
+
+    levels = 6
+    plan, imgs = _plan(gpu, oracle, SIZES, levels, oracle.MIRROR, 12)
+    px = sum(w * h for (w, h) in SIZES)
+    key = "pyramid:m%d:n%d:l%d:px2^%d" % (mode, len(SIZES), levels, math.ceil(math.log2(px)))
+    refs = [oracle.pyramid_decompose(im, levels, oracle.binomial5(), oracle.MIRROR, contract=1) for im in imgs]
+    for k in range(8 if mode == 0 else 4):
+        f = tmp_path / "choice.json"
+        f.write_text(json.dumps({key: [k, 0.0]}))
+        L.call("hgb_autotune_clear")
+        L.call("hgb_autotune_load", str(f).encode())
+        for i in range(len(SIZES)):
+            for l in range(1, levels):
+                plan.gauss(i, l).fill_(float("nan"))
+        plan.decompose(mode)
+        torch.cuda.synchronize()
+        for i, (g, lap) in enumerate(refs):
+            for l in range(levels):
+                assert np.array_equal(plan.gauss(i, l).cpu().numpy(), g[l]), (k, i, l)
+                if l + 1 < levels:
+                    assert np.array_equal(plan.lap(i, l).cpu().numpy(), lap[l]), (k, i, l)
+    L.call("hgb_autotune_clear")
+    st = C.c_int(-1)
+    L.call("hgb_device_status", C.byref(st))
+    assert st.value == 0
+    plan.close()
+
+
+def test_pyramid_autotuner_picks_and_keeps_a_choice(gpu, oracle, tmp_path):
+    """With autotuning on, the first decomposition times the configurations
+    and stores one choice per (launch form, batch shape); results stay exact."""
+    from hipacc_gb300 import _lib as L
+
+    L.call("hgb_autotune_clear")
+    gpu.autotune(True)
+    try:
+        plan, imgs = _plan(gpu, oracle, SIZES[:3], 5, oracle.MIRROR, 13)
+        n0 = L.load().hgb_autotune_count()
+        plan.decompose(0)
+        plan.decompose(1)
+        torch.cuda.synchronize()
+        assert L.load().hgb_autotune_count() == n0 + 2
+        for i, im in enumerate(imgs):
+            g, lap = oracle.pyramid_decompose(im, 5, oracle.binomial5(), oracle.MIRROR, contract=1)
+            assert np.array_equal(plan.lap(i, 0).cpu().numpy(), lap[0])
+            assert np.array_equal(plan.gauss(i, 4).cpu().numpy(), g[4])
+        f = tmp_path / "tuned.json"
+        L.call("hgb_autotune_save", str(f).encode())
+        assert "pyramid:m0" in f.read_text() and "pyramid:m1" in f.read_text()
+        plan.close()
+    finally:
+        gpu.autotune(False)
+        L.call("hgb_autotune_clear")
