@@ -68,6 +68,7 @@ using PyCfg2 = PyCfg<32, 32, 128>;
 using PyCfg3 = PyCfg<64, 32, 256>;
 constexpr int kPyCfgs = 4;
 constexpr int PY_TW = 64, PY_TH = 32;  // config 0, the collapse's tiles
+constexpr int kPyClaim = 4;            // tiles per claim of a persistent CTA
 
 struct LevelMeta {
   float *g;    // Gaussian level
@@ -97,7 +98,8 @@ struct PyrParams {
   unsigned int *abort;      // set when a tile failed: dependants stop waiting (persistent form)
   int *status;
   long long max_polls;      // limit of every bounded wait
-  int single;               // one tile per CTA (pyr_persistent_kernel)
+  int single;               // pyr_persistent_kernel: 0 persistent, 1 one tile per CTA, 2 static level 0
+  int nlevel0;              // tiles of level 0 (the head of the work-list)
   int inject_kind;          // wait test (hgb_pyramid_plan_wait_test): 0 none, 1 withhold, 2 no copy
   int inject_level;
   float mask[25];
@@ -194,10 +196,17 @@ __device__ bool pyr_tile(const PyrParams &p, const PyrTile t, float *stage, floa
                          int *ncx, int *ncy, uint64_t *bar, unsigned &phase, bool coherent) {
   // ---- stage the G_l box [by, by + BH) x [bx, bx + BW) with one TMA load
   if (threadIdx.x == 0) {
-    // in the persistent form G_l was written by other CTAs of this launch
-    // (generic stores, acquired by the level wait) and the previous tile's
-    // patch wrote `stage` with generic stores: order both before the copy
-    if (coherent) asm volatile("fence.proxy.async;" ::: "memory");
+    // in the single-launch forms the previous tile's patch wrote `stage` with
+    // generic stores, and a level above 0 was written by other CTAs of this
+    // launch (generic stores, acquired by the level wait): order them before
+    // the copy.  Level 0 was written before the launch and needs only the
+    // shared-memory fence.
+    if (coherent) {
+      if (t.level > 0)
+        asm volatile("fence.proxy.async;" ::: "memory");
+      else
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
     mbar_expect_tx(bar, C::BW * C::BH * 4);
     // wait test kind 2: the bytes are expected but no copy is issued, so the
     // barrier's phase never completes (nothing is in flight when the wait expires)
@@ -387,9 +396,28 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(cons
   }
   __syncthreads();
   unsigned phase = 0;
+  // single == 2 (a cooperative, co-resident grid): the level-0 tiles, which
+  // wait on nothing, are taken round-robin without an atomic; the later levels
+  // are claimed.  Otherwise every tile is claimed, kPyClaim consecutive tiles
+  // per atomic for persistent CTAs (the claim counter is one address for the
+  // whole launch); tiles are processed in list order.
+  int claim_base = 0, claim_left = 0;
+  int static_next = p.single == 2 ? (int)blockIdx.x : p.nlevel0;
   for (;;) {
     if (threadIdx.x == 0) {
-      const int t = (int)atomicAdd(p.work, 1u);
+      int t;
+      if (static_next < p.nlevel0) {
+        t = static_next;
+        static_next += gridDim.x;
+      } else {
+        if (claim_left == 0) {
+          const int chunk = p.single == 1 ? 1 : kPyClaim;
+          claim_base = (int)atomicAdd(p.work, (unsigned)chunk) + (p.single == 2 ? p.nlevel0 : 0);
+          claim_left = chunk;
+        }
+        t = claim_base++;
+        --claim_left;
+      }
       s_t = t;
       s_ok = 1;
       if (t < p.ntiles) {
@@ -423,7 +451,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(cons
     if (t >= p.ntiles || s_ok == 0) return;
     const PyrTile tl = p.tiles[t];
     if (s_ok == 2) {  // uniform: every thread read s_ok after the barrier
-      if (p.single) return;
+      if (p.single == 1) return;
       __syncthreads();  // s_t / s_ok are read before thread 0 claims again
       continue;
     }
@@ -433,7 +461,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(cons
     }
     __syncthreads();
     if (threadIdx.x == 0) red_release_add(&p.done[tl.img * p.levels + tl.level], 1u);
-    if (p.single) return;
+    if (p.single == 1) return;
   }
 }
 
@@ -712,9 +740,18 @@ static int launch_decompose(const hgb_pyramid_plan *P, int c, int mode, int sing
   if (mode == 0) {
     HGB_CHECK_CUDA(cudaMemsetAsync(P->d_ctrl, 0, ((size_t)P->n * P->levels + 2) * sizeof(unsigned int), st));
     p.single = single;
-    const int grid = single ? D.ntiles : std::min(D.persistent_ctas, D.ntiles);
+    p.nlevel0 = D.level_count[0];
+    const int grid = single == 1 ? D.ntiles : std::min(D.persistent_ctas, D.ntiles);
     cudaEvent_t ev = before_launch(st);
-    pyr_persistent_kernel<C><<<grid, C::NT, 0, st>>>(p);
+    if (single == 2) {
+      // co-residency of the whole grid is what makes the static level-0 share
+      // safe: a cooperative launch fails instead of running a partial grid
+      void *args[] = {(void *)&p};
+      HGB_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)pyr_persistent_kernel<C>, dim3(grid), dim3(C::NT),
+                                                 args, 0, st));
+    } else {
+      pyr_persistent_kernel<C><<<grid, C::NT, 0, st>>>(p);
+    }
     return after_launch("pyr_persistent_kernel", st, ev);
   }
   for (int l = 0; l + 1 < P->levels; ++l) {
@@ -750,7 +787,7 @@ int hgb_pyramid_decompose(hgb_pyramid_plan *P, int mode, void *stream) {
     while ((int64_t(1) << lg) < px) ++lg;
     char key[96];
     snprintf(key, sizeof(key), "pyramid:m%d:n%d:l%d:px2^%d", mode, P->n, P->levels, lg);
-    const int ncfg = mode == 0 ? 2 * kPyCfgs : kPyCfgs;
+    const int ncfg = mode == 0 ? 3 * kPyCfgs : kPyCfgs;
     return autotune_run(key, ncfg, st, [&](int k) {
       return launch_cfg(P, k % kPyCfgs, mode, mode == 0 ? k / kPyCfgs : 0, st);
     });

@@ -19,6 +19,9 @@
 // combine of the per-block partials.
 #include <algorithm>
 
+#include <cstdio>
+
+#include "autotune.h"
 #include "reduce_common.cuh"
 #include "tma.cuh"
 
@@ -232,7 +235,12 @@ struct SobelTmaParams {
   unsigned int *ticket;
 };
 
-constexpr int T_TW = 128, T_R = 32, T_WARPS = 4, T_TH = T_R * T_WARPS;
+// the tile is 128 x 128 outputs in either configuration; the autotuner picks
+// the rows per warp: 32 rows for 4 warps, or 16 rows for 8 warps (a shorter
+// serial stencil per warp after the tile lands, twice the warps per SM)
+constexpr int T_TW = 128, T_TH = 128;
+constexpr int kSobelWarps[] = {4, 8};
+constexpr int kSobelCfgs = 2;
 constexpr int T_SW = 160, T_SH = T_TH + 2, T_STAGE = T_SW * T_SH;
 constexpr int T_STAGE_PAD = (T_STAGE + 127) / 128 * 128;
 
@@ -315,7 +323,9 @@ __device__ __forceinline__ void sobel_tile(const SobelParams &p, const uint8_t *
   }
 }
 
+template <int T_WARPS>
 __global__ void __launch_bounds__(T_WARPS * 32) sobel3_tma_kernel(const __grid_constant__ SobelTmaParams P) {
+  constexpr int T_R = T_TH / T_WARPS;
   __shared__ __align__(128) uint8_t tile[T_STAGE_PAD];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t s_sum[T_WARPS], s_max[T_WARPS];
@@ -514,9 +524,17 @@ extern "C" int hgb_sobel_mag(const hgb_view *in, const hgb_view *out, const int 
         P.acc = ws.acc + kSlotSobel;
         P.ticket = ws.tickets + 0;
       }
-      cudaEvent_t ev = before_launch(st);
-      sobel3_tma_kernel<<<P.ntiles, T_WARPS * 32, 0, st>>>(P);
-      return after_launch("sobel3_tma_kernel", st, ev);
+      char key[96];
+      snprintf(key, sizeof(key), "sobel3:%dx%dx%d", 1 << (32 - __builtin_clz((unsigned)p.w)),
+               1 << (32 - __builtin_clz((unsigned)p.h)), in->batch);
+      return autotune_run(key, kSobelCfgs, st, [&](int cfg) {
+        cudaEvent_t ev = before_launch(st);
+        if (kSobelWarps[cfg] == 8)
+          sobel3_tma_kernel<8><<<P.ntiles, 256, 0, st>>>(P);
+        else
+          sobel3_tma_kernel<4><<<P.ntiles, 128, 0, st>>>(P);
+        return after_launch("sobel3_tma_kernel", st, ev);
+      });
     }
   }
   cudaEvent_t ev = before_launch(st);

@@ -31,6 +31,65 @@ def test_sobel_bitexact(gpu, oracle, b, hw):
     assert s == oracle.reduce_sum_u8(ref) and m == oracle.reduce_max_u8(ref)
 
 
+@pytest.mark.parametrize("b", [1, 2, 3, 4])
+@pytest.mark.parametrize("hw", [(129, 129), (200, 301), (1, 1), (3, 1000), (1001, 333), (35, 4097), (257, 128)])
+def test_sobel_pitched_tma_path(gpu, oracle, b, hw):
+    """Rows padded to a multiple of 16 bytes make any width TMA-legal: ragged
+    right and bottom tiles and one-row images through the staged fast path,
+    one image and a batch of three."""
+    rng = np.random.default_rng(hash(("p", b, hw)) % 2**32)
+    h, w = hw
+    wp = (w + 15) // 16 * 16 + 16
+    imgs = rng.integers(0, 256, (3, h, w), dtype=np.uint8)
+    dev = torch.zeros((3, h, wp), dtype=torch.uint8, device="cuda")
+    dev[:, :, :w] = torch.from_numpy(imgs).cuda()
+    out = torch.full((3, h, wp), 7, dtype=torch.uint8, device="cuda")
+    for batch in (False, True):
+        s = torch.zeros(1, dtype=torch.int64, device="cuda")
+        m = torch.zeros(1, dtype=torch.int32, device="cuda")
+        src = dev[:, :, :w] if batch else dev[0, :, :w]
+        dst = out[:, :, :w] if batch else out[0, :, :w]
+        gpu.sobel_mag(src, dst, boundary=b, const=17, sum_out=s, max_out=m)
+        torch.cuda.synchronize()
+        refs = [oracle.sobel_mag(imgs[i], boundary=b, const=17) for i in range(3 if batch else 1)]
+        got = out.cpu().numpy()
+        for i, ref in enumerate(refs):
+            assert np.array_equal(got[i, :, :w], ref), (batch, i)
+            assert np.all(got[i, :, w:] == 7)  # nothing written past the width
+        assert s.item() == sum(int(r.astype(np.uint64).sum()) for r in refs)
+        assert m.item() == max(int(r.max()) for r in refs)
+
+
+@pytest.mark.parametrize("cfg", [0, 1])
+def test_sobel_every_tile_configuration(gpu, oracle, cfg, tmp_path):
+    """Each configuration the autotuner can choose for the staged Sobel (rows
+    per warp), forced through a loaded choice file, is bit-exact."""
+    import json
+
+    from hipacc_gb300 import _lib as L
+
+    rng = np.random.default_rng(40 + cfg)
+    for (h, w) in [(777, 1001), (512, 512), (4096, 4096)]:
+        img = rng.integers(0, 256, (h, w), dtype=np.uint8)
+        wp = (w + 15) // 16 * 16
+        dev = torch.zeros((h, wp), dtype=torch.uint8, device="cuda")
+        dev[:, :w] = torch.from_numpy(img).cuda()
+        out = torch.zeros((h, wp), dtype=torch.uint8, device="cuda")
+        key = "sobel3:%dx%dx1" % (1 << w.bit_length(), 1 << h.bit_length())
+        f = tmp_path / "choice.json"
+        f.write_text(json.dumps({key: [cfg, 0.0]}))
+        L.call("hgb_autotune_clear")
+        L.call("hgb_autotune_load", str(f).encode())
+        s = torch.zeros(1, dtype=torch.int64, device="cuda")
+        m = torch.zeros(1, dtype=torch.int32, device="cuda")
+        gpu.sobel_mag(dev[:, :w], out[:, :w], boundary=3, sum_out=s, max_out=m)
+        torch.cuda.synchronize()
+        L.call("hgb_autotune_clear")
+        ref = oracle.sobel_mag(img, boundary=3)
+        assert np.array_equal(out[:, :w].cpu().numpy(), ref), (h, w)
+        assert s.item() == int(ref.astype(np.uint64).sum()) and m.item() == int(ref.max())
+
+
 def test_sobel_4096_mirror(gpu, oracle):
     """The 4096x4096 u8 Sobel with MIRROR and the u64 sum / u8 max."""
     rng = np.random.default_rng(2)

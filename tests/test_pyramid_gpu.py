@@ -181,8 +181,9 @@ def test_pyramid_wait_test_arguments(gpu, oracle):
 @pytest.mark.parametrize("mode", [0, 1])
 def test_pyramid_every_tile_configuration(gpu, oracle, mode, tmp_path):
     """Every configuration the autotuner can choose for the fused launches
-    (tile shape and threads; for the single launch also persistent CTAs or one
-    CTA per tile), forced through a loaded choice file, is bit-exact."""
+    (tile shape and threads; for the single launch also persistent claiming
+    CTAs, one CTA per tile, or a cooperative grid sharing level 0 statically),
+    forced through a loaded choice file, is bit-exact."""
     import json
     import math
 
@@ -193,7 +194,7 @@ def test_pyramid_every_tile_configuration(gpu, oracle, mode, tmp_path):
     px = sum(w * h for (w, h) in SIZES)
     key = "pyramid:m%d:n%d:l%d:px2^%d" % (mode, len(SIZES), levels, math.ceil(math.log2(px)))
     refs = [oracle.pyramid_decompose(im, levels, oracle.binomial5(), oracle.MIRROR, contract=1) for im in imgs]
-    for k in range(8 if mode == 0 else 4):
+    for k in range(12 if mode == 0 else 4):
         f = tmp_path / "choice.json"
         f.write_text(json.dumps({key: [k, 0.0]}))
         L.call("hgb_autotune_clear")
@@ -240,3 +241,41 @@ def test_pyramid_autotuner_picks_and_keeps_a_choice(gpu, oracle, tmp_path):
     finally:
         gpu.autotune(False)
         L.call("hgb_autotune_clear")
+
+
+@pytest.mark.parametrize("k", [0, 4, 8])
+def test_pyramid_single_launch_in_a_graph(gpu, oracle, k, tmp_path):
+    """Each form of the single launch (persistent claiming, one CTA per tile,
+    cooperative static level 0) is recorded into a CUDA graph and replayed."""
+    import json
+    import math
+
+    from hipacc_gb300 import _lib as L
+
+    levels = 6
+    plan, imgs = _plan(gpu, oracle, SIZES, levels, oracle.MIRROR, 14)
+    px = sum(w * h for (w, h) in SIZES)
+    key = "pyramid:m0:n%d:l%d:px2^%d" % (len(SIZES), levels, math.ceil(math.log2(px)))
+    f = tmp_path / "choice.json"
+    f.write_text(json.dumps({key: [k, 0.0]}))
+    L.call("hgb_autotune_clear")
+    L.call("hgb_autotune_load", str(f).encode())
+    try:
+        s = torch.cuda.Stream()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            plan.decompose(0, stream=s)
+        for i in range(len(SIZES)):
+            for l in range(levels - 1):
+                plan.lap(i, l).fill_(float("nan"))
+        torch.cuda.synchronize()
+        g.replay()
+        g.replay()
+        torch.cuda.synchronize()
+        for i, im in enumerate(imgs):
+            _, lap = oracle.pyramid_decompose(im, levels, oracle.binomial5(), oracle.MIRROR, contract=1)
+            for l in range(levels - 1):
+                assert np.array_equal(plan.lap(i, l).cpu().numpy(), lap[l]), (k, i, l)
+    finally:
+        L.call("hgb_autotune_clear")
+        plan.close()
