@@ -155,22 +155,45 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
       xs[c] = (ry == (int)0x80000000 || rx == (int)0x80000000) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
     }
     __syncthreads();
-    // y1 on the tile + bilateral halo; a halo cell outside the image is y1 at
-    // the remapped position (the bilateral reads y1 through the boundary)
-    for (int c = threadIdx.x; c < YS_W * YS_H; c += C5_T) {
-      const int r = c / YS_W, q = c - r * YS_W;
-      const int vy = Y0 - C5_BR + r, vx = X0 - C5_BR + q;
-      const int ry = remap_c5(bm, vy, H), rx = remap_c5(bm, vx, W);
-      float acc = 0.0f;
-      if (ry != (int)0x80000000 && rx != (int)0x80000000) {
-        // staged x coordinate of (ry - 3, rx - 3)
-        const int sy = ry - C5_MR - (Y0 - R), sx = rx - C5_MR - (X0 - R);
+    // y1 on the tile + bilateral halo, four adjacent cells per thread from one
+    // row window of the staged x per mask row (taps row-major, as one cell at a
+    // time); a halo cell outside the image is y1 at the remapped position (the
+    // bilateral reads y1 through the boundary)
+    static_assert(YS_W % 4 == 0 && YS_H * (YS_W / 4) <= C5_T, "one group of four cells per thread");
+    for (int g = threadIdx.x; g < YS_H * (YS_W / 4); g += C5_T) {
+      const int r = g / (YS_W / 4), q4 = (g - r * (YS_W / 4)) * 4;
+      const int vy = Y0 - C5_BR + r, vx = X0 - C5_BR + q4;
+      if (vy >= 0 && vy < H && vx >= 0 && vx + 3 < W) {
+        // staged rows r .. r + 6, columns q4 .. q4 + 9 (R = MR + BR)
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-        for (int my = 0; my < C5_MK; ++my)
+        for (int my = 0; my < C5_MK; ++my) {
+          float v[4 + C5_MK - 1];
 #pragma unroll
-          for (int mx = 0; mx < C5_MK; ++mx) acc = __fmaf_rn(msk[my * C5_MK + mx], xs[(sy + my) * XS_W + sx + mx], acc);
+          for (int i = 0; i < 4 + C5_MK - 1; ++i) v[i] = xs[(r + my) * XS_W + q4 + i];
+#pragma unroll
+          for (int mx = 0; mx < C5_MK; ++mx)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[j] = __fmaf_rn(msk[my * C5_MK + mx], v[j + mx], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ys[r * YS_W + q4 + j] = acc[j];
+        continue;
       }
-      ys[c] = acc;
+      for (int j = 0; j < 4; ++j) {
+        const int ry = remap_c5(bm, vy, H), rx = remap_c5(bm, vx + j, W);
+        float acc = 0.0f;
+        if (ry != (int)0x80000000 && rx != (int)0x80000000) {
+          // staged x coordinate of (ry - 3, rx - 3)
+          const int sy = ry - C5_MR - (Y0 - R), sx = rx - C5_MR - (X0 - R);
+#pragma unroll
+          for (int my = 0; my < C5_MK; ++my)
+#pragma unroll
+            for (int mx = 0; mx < C5_MK; ++mx)
+              acc = __fmaf_rn(msk[my * C5_MK + mx], xs[(sy + my) * XS_W + sx + mx], acc);
+        }
+        ys[r * YS_W + q4 + j] = acc;
+      }
     }
   } else {
     const float *y1 = p.y1 + (int64_t)b * p.ib;
@@ -278,13 +301,20 @@ __device__ __forceinline__ int preimages(int mode, int j, int n, int rad, int *o
 }
 
 __global__ void __launch_bounds__(C5_T) c5_bilateral_adjoint_kernel(const __grid_constant__ C5Params p) {
-  __shared__ float sa[YS_W * YS_H], sy[YS_W * YS_H], s1[YS_W * YS_H];
+  // staged per pixel of the tile + radius: (q y1, a, a q y, q y) with
+  // q = sqrt(c log2 e), so that a tap's weight is exp2(lsm - d'^2) for the
+  // scaled difference d' = q (y1_j - y1_p)
+  __shared__ float4 s4[YS_W * YS_H];
   __shared__ float sbuf[32];
   __shared__ double dsh[C5_T];
   const int W = p.w, H = p.h, bm = p.bmode;
   float c, k2;
   sigma_consts(p, c, k2);
   const float c2 = 2.0f * c;
+  const float q = sqrtf(-k2), inv_q = 1.0f / q;
+  // 2c (y1_j - y_p)(y1_j - y1_p) = C2S (q y1_j - q y_p) d' with C2S = 2c / q^2 = 2 ln 2
+  constexpr float C2S = 1.3862943611198906f;
+  const float inv_q3 = inv_q * inv_q * inv_q;
   float dc = 0.0f;
   for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
   int b, X0, Y0;
@@ -292,67 +322,77 @@ __global__ void __launch_bounds__(C5_T) c5_bilateral_adjoint_kernel(const __grid
   const int64_t base = (int64_t)b * p.ib;
   __syncthreads();  // the previous tile's reads are done
   // in-image cells of [X0-4, X0+TW+4) x [Y0-4, Y0+TH+4); others are never read
-  for (int c = threadIdx.x; c < YS_W * YS_H; c += C5_T) {
-    const int r = c / YS_W, q = c - r * YS_W;
-    const int gy = Y0 - C5_BR + r, gx = X0 - C5_BR + q;
+  for (int cc = threadIdx.x; cc < YS_W * YS_H; cc += C5_T) {
+    const int r = cc / YS_W, qx = cc - r * YS_W;
+    const int gy = Y0 - C5_BR + r, gx = X0 - C5_BR + qx;
     if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
       const int64_t o = base + (int64_t)gy * p.ip + gx;
-      sa[c] = p.a[o];
-      sy[c] = p.y[o];
-      s1[c] = p.y1[o];
+      const float a = p.a[o], uy = q * p.y[o];
+      s4[cc] = make_float4(q * p.y1[o], a, a * uy, uy);
     }
   }
   __syncthreads();
   const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
-  auto S = [&](const float *arr, int gy, int gx) { return arr[(gy - Y0 + C5_BR) * YS_W + gx - X0 + C5_BR]; };
+  auto S = [&](int gy, int gx) { return s4[(gy - Y0 + C5_BR) * YS_W + gx - X0 + C5_BR]; };
   for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
     const int jx = X0 + tx, jy = Y0 + py;
     if (jx >= W || jy >= H) continue;
-    const float aj = S(sa, jy, jx), yj = S(sy, jy, jx), y1j = S(s1, jy, jx);
-    float dn = 0.0f, ctr = 0.0f;
+    const int sj = (py + C5_BR) * YS_W + tx + C5_BR;
+    const float4 J = s4[sj];
+    const float u1j = J.x, aj = J.y, uyj = J.w;
+    float dn = 0.0f, s1 = 0.0f, s2 = 0.0f;
     const bool inner = jx >= C5_BR && jx < W - C5_BR && jy >= C5_BR && jy < H - C5_BR;
     if (inner && p.symmetric) {
 #pragma unroll 3
       for (int oy = 0; oy < C5_BK; ++oy)
 #pragma unroll
         for (int ox = 0; ox < C5_BK; ++ox) {
-          // p = j - o; tap o of p reads j, tap -o of j reads p; same weight
-          const int qy = jy - (oy - C5_BR), qx = jx - (ox - C5_BR);
-          const float ap = S(sa, qy, qx), ypp = S(sy, qy, qx), y1p = S(s1, qy, qx);
-          const float d = y1j - y1p;
-          const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
-          dn = __fmaf_rn(ap * e, 1.0f - c2 * (y1j - ypp) * d, dn);
-          const float u = e * (y1p - yj);
-          ctr = __fmaf_rn(u, -c2 * d, ctr);  // (y1p - yj) 2c (y1p - y1j)
-          dc = __fmaf_rn(aj * u, -(d * d), dc);
+          // p = j - o; tap o of p reads j, tap -o of j reads p; one weight
+          const float4 P = s4[sj - (oy - C5_BR) * YS_W - (ox - C5_BR)];
+          const float d = u1j - P.x;
+          const float e = ex2f(__fmaf_rn(-d, d, p.lsm[oy * C5_BK + ox]));
+          // neighbour term a_p e (1 - 2c (y1_j - y_p) d)
+          const float t = __fmaf_rn(u1j, P.y, -P.z);
+          dn = __fmaf_rn(e, __fmaf_rn(-C2S * d, t, P.y), dn);
+          // j's own tap -o: e (y1_p - y_j) d' into the centre and dL/dc sums
+          const float wd = e * (P.x - uyj) * d;
+          s1 += wd;
+          s2 = __fmaf_rn(wd, d, s2);
         }
-    } else {
-      // centre term and dL/dc over j's own taps
-      for (int oy = 0; oy < C5_BK; ++oy)
-        for (int ox = 0; ox < C5_BK; ++ox) {
-          const int qy = remap_c5(bm, jy + oy - C5_BR, H), qx = remap_c5(bm, jx + ox - C5_BR, W);
-          const float v = (qy == (int)0x80000000 || qx == (int)0x80000000) ? 0.0f : S(s1, qy, qx);
-          const float d = v - y1j;
-          const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
-          const float u = e * (v - yj);
-          ctr = __fmaf_rn(u, c2 * d, ctr);
-          dc = __fmaf_rn(aj * u, -(d * d), dc);
-        }
-      // neighbour term gathered over the pre-images of j
-      int prx[1 + C5_BR], pry[1 + C5_BR];
-      const int nx = preimages(bm, jx, W, C5_BR, prx), ny = preimages(bm, jy, H, C5_BR, pry);
-      for (int iy = 0; iy < ny; ++iy)
-        for (int ix = 0; ix < nx; ++ix)
-          for (int oy = 0; oy < C5_BK; ++oy)
-            for (int ox = 0; ox < C5_BK; ++ox) {
-              const int qy = pry[iy] - (oy - C5_BR), qx = prx[ix] - (ox - C5_BR);
-              if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
-              const float ap = S(sa, qy, qx), ypp = S(sy, qy, qx), y1p = S(s1, qy, qx);
-              const float d = y1j - y1p;
-              const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
-              dn = __fmaf_rn(ap * e, 1.0f - c2 * (y1j - ypp) * d, dn);
-            }
+      // centre term a_j sum e (y1_p - y_j) 2c (y1_p - y1_j) = -C2S a_j s1;
+      // dL/dc over j's taps: -a_j s2 / q^3
+      dc = __fmaf_rn(-aj * inv_q3, s2, dc);
+      p.dy1[base + (int64_t)jy * p.ip + jx] = __fmaf_rn(-C2S * aj, s1, dn);
+      continue;
     }
+    const float y1j = u1j * inv_q, yj = uyj * inv_q;
+    float ctr = 0.0f;
+    // centre term and dL/dc over j's own taps
+    for (int oy = 0; oy < C5_BK; ++oy)
+      for (int ox = 0; ox < C5_BK; ++ox) {
+        const int qy = remap_c5(bm, jy + oy - C5_BR, H), qx = remap_c5(bm, jx + ox - C5_BR, W);
+        const float v = (qy == (int)0x80000000 || qx == (int)0x80000000) ? 0.0f : S(qy, qx).x * inv_q;
+        const float d = v - y1j;
+        const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
+        const float u = e * (v - yj);
+        ctr = __fmaf_rn(u, c2 * d, ctr);
+        dc = __fmaf_rn(aj * u, -(d * d), dc);
+      }
+    // neighbour term gathered over the pre-images of j
+    int prx[1 + C5_BR], pry[1 + C5_BR];
+    const int nx = preimages(bm, jx, W, C5_BR, prx), ny = preimages(bm, jy, H, C5_BR, pry);
+    for (int iy = 0; iy < ny; ++iy)
+      for (int ix = 0; ix < nx; ++ix)
+        for (int oy = 0; oy < C5_BK; ++oy)
+          for (int ox = 0; ox < C5_BK; ++ox) {
+            const int qy = pry[iy] - (oy - C5_BR), qx = prx[ix] - (ox - C5_BR);
+            if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+            const float4 P = S(qy, qx);
+            const float y1p = P.x * inv_q, ypp = P.w * inv_q;
+            const float d = y1j - y1p;
+            const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
+            dn = __fmaf_rn(P.y * e, 1.0f - c2 * (y1j - ypp) * d, dn);
+          }
     p.dy1[base + (int64_t)jy * p.ip + jx] = __fmaf_rn(aj, ctr, dn);
   }
   }  // tiles
@@ -396,41 +436,73 @@ __global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_cons
   }
   __syncthreads();
   auto D = [&](int gy, int gx) { return sd[(gy - Y0 + C5_MR) * DS_W + gx - X0 + C5_MR]; };
-  const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
-  for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
-    const int ix = X0 + tx, iy = Y0 + py;
-    if (ix >= W || iy >= H) continue;
-    float acc = 0.0f;
-    const bool inner = ix >= C5_MR && ix < W - C5_MR && iy >= C5_MR && iy < H - C5_MR;
-    if (inner) {
+  // a thread per pair of horizontally adjacent pixels: each staged row window
+  // serves both pixels' taps (taps in the same row-major order per pixel)
+  static_assert(C5_TW * C5_TH == 2 * C5_T, "two pixels per thread");
+  const int tx2 = threadIdx.x % (C5_TW / 2), py = threadIdx.x / (C5_TW / 2);
+  const int ix0 = X0 + 2 * tx2, iy = Y0 + py;
+  const bool cst = bm == HGB_BOUNDARY_CONSTANT;
+  if (iy < H && ix0 < W) {
+    const bool inner2 = ix0 >= C5_MR && ix0 + 1 < W - C5_MR && iy >= C5_MR && iy < H - C5_MR;
+    if (inner2) {
+      float acc0 = 0.0f, acc1 = 0.0f;
 #pragma unroll
-      for (int oy = 0; oy < C5_MK; ++oy)
+      for (int oy = 0; oy < C5_MK; ++oy) {
+        // grad_out row iy - (oy - 3), columns ix0 - 3 .. ix0 + 4
+        const float *row = &sd[(py + 2 * C5_MR - oy) * DS_W + 2 * tx2];
+        float v[2 + C5_MK - 1];
 #pragma unroll
-        for (int ox = 0; ox < C5_MK; ++ox) acc = __fmaf_rn(msk[oy * C5_MK + ox], D(iy - oy + C5_MR, ix - ox + C5_MR), acc);
-    } else {
-      int prx[1 + C5_MR], pry[1 + C5_MR];
-      const int nx = preimages(bm, ix, W, C5_MR, prx), ny = preimages(bm, iy, H, C5_MR, pry);
-      for (int a = 0; a < ny; ++a)
-        for (int c = 0; c < nx; ++c)
-          for (int oy = 0; oy < C5_MK; ++oy)
-            for (int ox = 0; ox < C5_MK; ++ox) {
-              const int jy = pry[a] - (oy - C5_MR), jx = prx[c] - (ox - C5_MR);
-              if (jx < 0 || jx >= W || jy < 0 || jy >= H) continue;
-              acc = __fmaf_rn(msk[oy * C5_MK + ox], D(jy, jx), acc);
-            }
-    }
-    p.dx[(int64_t)b * p.dxb + (int64_t)iy * p.dxp + ix] = acc;
-    if (p.fuse_dmask) {
-      const float dj = D(iy, ix);
-      const bool cst = bm == HGB_BOUNDARY_CONSTANT;
-#pragma unroll
-      for (int oy = 0; oy < C5_MK; ++oy)
+        for (int i = 0; i < 2 + C5_MK - 1; ++i) v[i] = row[i];
 #pragma unroll
         for (int ox = 0; ox < C5_MK; ++ox) {
-          const int vy = iy + oy - C5_MR, vx = ix + ox - C5_MR;
-          if (cst && (vx < 0 || vx >= W || vy < 0 || vy >= H)) continue;
-          dm[oy * C5_MK + ox] = __fmaf_rn(dj, sx[(vy - Y0 + C5_MR) * DS_W + vx - X0 + C5_MR], dm[oy * C5_MK + ox]);
+          acc0 = __fmaf_rn(msk[oy * C5_MK + ox], v[2 * C5_MR - ox], acc0);
+          acc1 = __fmaf_rn(msk[oy * C5_MK + ox], v[2 * C5_MR - ox + 1], acc1);
         }
+      }
+      float *dx = p.dx + (int64_t)b * p.dxb + (int64_t)iy * p.dxp + ix0;
+      dx[0] = acc0;
+      dx[1] = acc1;
+    } else {
+      for (int j = 0; j < 2; ++j) {
+        const int ix = ix0 + j;
+        if (ix >= W) break;
+        float acc = 0.0f;
+        int prx[1 + C5_MR], pry[1 + C5_MR];
+        const int nx = preimages(bm, ix, W, C5_MR, prx), ny = preimages(bm, iy, H, C5_MR, pry);
+        for (int aa = 0; aa < ny; ++aa)
+          for (int c = 0; c < nx; ++c)
+            for (int oy = 0; oy < C5_MK; ++oy)
+              for (int ox = 0; ox < C5_MK; ++ox) {
+                const int jy = pry[aa] - (oy - C5_MR), jx = prx[c] - (ox - C5_MR);
+                if (jx < 0 || jx >= W || jy < 0 || jy >= H) continue;
+                acc = __fmaf_rn(msk[oy * C5_MK + ox], D(jy, jx), acc);
+              }
+        p.dx[(int64_t)b * p.dxb + (int64_t)iy * p.dxp + ix] = acc;
+      }
+    }
+    if (p.fuse_dmask) {
+      const float dj0 = D(iy, ix0), dj1 = ix0 + 1 < W ? D(iy, ix0 + 1) : 0.0f;
+      const bool inner_taps = ix0 >= C5_MR && ix0 + 1 < W - C5_MR && iy >= C5_MR && iy < H - C5_MR;
+#pragma unroll
+      for (int oy = 0; oy < C5_MK; ++oy) {
+        // x through the boundary, row iy + oy - 3, columns ix0 - 3 .. ix0 + 4
+        const float *row = &sx[(py + oy) * DS_W + 2 * tx2];
+        float v[2 + C5_MK - 1];
+#pragma unroll
+        for (int i = 0; i < 2 + C5_MK - 1; ++i) v[i] = row[i];
+        const int vy = iy + oy - C5_MR;
+#pragma unroll
+        for (int ox = 0; ox < C5_MK; ++ox) {
+          float t0 = v[ox], t1 = v[ox + 1];
+          if (cst && !inner_taps) {  // CONSTANT taps outside the image carry no gradient
+            const int vx = ix0 + ox - C5_MR;
+            const bool yo = vy < 0 || vy >= H;
+            if (yo || vx < 0 || vx >= W) t0 = 0.0f;
+            if (yo || vx + 1 < 0 || vx + 1 >= W) t1 = 0.0f;
+          }
+          dm[oy * C5_MK + ox] = __fmaf_rn(dj1, t1, __fmaf_rn(dj0, t0, dm[oy * C5_MK + ox]));
+        }
+      }
     }
   }
   }  // tiles
