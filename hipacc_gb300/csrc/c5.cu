@@ -17,17 +17,41 @@
 // from every (p, o) with r(p + o) = q, found per axis among the virtual
 // positions within the radius of the border (CLAMP and MIRROR send several
 // virtual positions to an edge pixel; CONSTANT taps carry no gradient).  The
-// bilateral weights are recomputed in the adjoint, never stored.  Inside the
-// image the spatial mask's symmetry makes one exponential serve both the
-// neighbour term (weight of tap o at p = j - o) and the centre term (tap -o
-// at j).  Reductions (loss, dL/dc, dL/dmask) use per-block partials combined
-// in FP64 in block order by the block that takes the last ticket.
+// bilateral weights are recomputed in the adjoint, never stored.
 //
-// Launch forms: mode 0 = three batched kernels (forward with the conv
-// recomputed on its halo and the loss gradient in the epilogue, bilateral
-// adjoint, conv adjoint with the mask gradient); mode 1 = the unfused chain
-// per image (conv, bilateral forward, loss gradient, bilateral adjoint without
-// the symmetry reuse, conv adjoint, mask gradient) for comparison.
+// The bilateral works on values scaled by q = sqrt(c log2 e): with u = q y1 a
+// tap's weight is exp2(lsm_o - (u_q - u_p)^2) (lsm = log2 smask), and with
+// u_y = q y the factor 2c (y1_q - y_p)(y1_q - y1_p) is C2S (u_q - u_yp)(u_q -
+// u_p) with C2S = 2 ln 2.
+//
+// Fused form (mode 0): three persistent kernels over 64 x 16 tiles, 16 x 16
+// threads with four horizontally adjacent pixels each, two pixels per packed
+// f32x2 operation (every lane rounded like the scalar instruction):
+//  1. forward: x staged with a radius of 7 through the boundary; y1 on the
+//     tile plus the bilateral radius, eight cells per thread; the bilateral on
+//     u (one ex2 and four packed lane operations per tap and pixel pair); the
+//     loss and its gradient.  It writes per pixel the float4
+//     (u, a, -a u_y, u_y).
+//  2. bilateral adjoint: away from the band of radius 4 along the image edges,
+//     pixel j gathers from its neighbours p = j - o with the weight of tap o
+//     at p, which by the spatial mask's point symmetry is also the weight of
+//     j's own tap -o: one ex2 and ten packed operations per tap serve the
+//     neighbour term, the centre term and dL/dc.  Band pixels, whose taps
+//     cross the edge, go through the pre-images one pixel per thread, as an
+//     equal contiguous share of the batch's band list per CTA after its tiles,
+//     so the tiles cost the same and the walk has no tail of border tiles.
+//  3. convolution adjoint: grad_in as the transposed convolution away from the
+//     band of radius 3, and the mask gradient accumulated per pair of taps in
+//     packed registers; band pixels again from a flat list.
+// Every CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...; the
+// reductions (loss, dL/dc, dL/dmask) keep per-thread and per-CTA partials in
+// a fixed assignment and are combined in FP64 in block order by the CTA that
+// takes the last ticket, so results do not change from run to run.
+//
+// Unfused form (mode 1): the chain per image as a kernel-per-operator
+// framework launches it (conv, bilateral forward, loss gradient, bilateral
+// adjoint without the symmetry reuse, conv adjoint, mask gradient), one pixel
+// per thread, for comparison.
 // Boundary CLAMP, MIRROR or CONSTANT(0); images at least 8 x 8.
 #include <algorithm>
 #include <cmath>
@@ -38,26 +62,48 @@
 namespace hgb {
 namespace {
 
-constexpr int C5_TW = 32, C5_TH = 16, C5_T = 256;
+constexpr int C5_T = 256;
 constexpr int C5_MK = 7, C5_MR = 3;  // conv mask
 constexpr int C5_BK = 9, C5_BR = 4;  // bilateral
-// staged regions
-constexpr int XS_W = C5_TW + 2 * (C5_MR + C5_BR), XS_H = C5_TH + 2 * (C5_MR + C5_BR);  // x for the fused forward
-constexpr int YS_W = C5_TW + 2 * C5_BR, YS_H = C5_TH + 2 * C5_BR;                      // y1 / a / y (radius 4)
-constexpr int DS_W = C5_TW + 2 * C5_MR, DS_H = C5_TH + 2 * C5_MR;                      // dy1 / x (radius 3)
+constexpr int C5_OUT = (int)0x80000000;  // remap result of a CONSTANT tap outside the image
+constexpr float C2S = 1.3862943611198906f;  // 2 ln 2
+// unfused kernels: 32 x 16 tiles, one pixel per thread
+constexpr int U_TW = 32, U_TH = 16;
+constexpr int UY_W = U_TW + 2 * C5_BR, UY_H = U_TH + 2 * C5_BR;  // y1 / a / y (radius 4)
+constexpr int UD_W = U_TW + 2 * C5_MR, UD_H = U_TH + 2 * C5_MR;  // dy1 / x (radius 3)
+// fused kernels: 64 x 16 tiles, four pixels per thread
+constexpr int F_TW = 64, F_TH = 16, F_GX = F_TW / 4;
+constexpr int FX_R = C5_MR + C5_BR;                          // radius of the staged x
+constexpr int FX_W = F_TW + 16, FX_H = F_TH + 2 * FX_R;      // x: columns X0-8 .. X0+71, rows Y0-7 ..
+constexpr int FY_W = F_TW + 2 * C5_BR, FY_H = F_TH + 2 * C5_BR;  // u / staged pairs: columns X0-4 .., rows Y0-4 ..
+constexpr int FC_W = F_TW + 8, FC_H = F_TH + 2 * C5_MR;      // dy1 / x pairs: columns X0-4 .., rows Y0-3 ..
+static_assert(F_GX * F_TH == C5_T, "16 x 16 threads");
+// Staged rows of pairs are skewed by one element every 8 (16-byte elements)
+// or every 16 (8-byte elements): a thread reads positions 4 tx + s, and
+// without the skew the 8 (16) lanes of one shared-memory phase would fall on
+// 2 (4) bank groups.
+constexpr int SQ_W = FY_W + FY_W / 8;   // float4 pairs (u, a)
+constexpr int SB_W = FY_W + FY_W / 16;  // float2 pairs (B)
+constexpr int SC_W = FC_W + FC_W / 16;  // float2 pairs (dy1, x)
+__host__ __device__ constexpr int skew8(int k) { return k + (k >> 3); }
+__host__ __device__ constexpr int skew16(int k) { return k + (k >> 4); }
+static_assert(skew8(FY_W - 1) < SQ_W && skew16(FY_W - 1) < SB_W && skew16(FC_W - 1) < SC_W, "skewed rows");
+static_assert(FY_H * (FY_W / 8) <= C5_T, "one group of eight y1 cells per thread");
 
 struct C5Params {
   const float *x, *t;
   int64_t xp, tp, xb, tb;  // pitches / batch strides in floats
-  float *y1, *y, *a, *dy1, *dx;
-  int64_t ip, ib;          // pitch / batch stride of the intermediates and dx (floats)
+  float4 *pk;              // fused: per pixel (u, a, -a u_y, u_y)
+  float *y1, *y, *a;       // unfused intermediates
+  float *dy1, *dx;
+  int64_t ip, ib;          // pitch / batch stride of the intermediates, in elements
   int64_t dxp, dxb;
   int w, h, batch;
   int bmode;
+  int vec_x, vec_dx;       // rows of x / grad_x allow aligned float4 accesses
   const float *mask_dev;   // 49
   const float *sigma_dev;  // 1
-  float lsm[C5_BK * C5_BK];  // log2(smask)
-  float sm[C5_BK * C5_BK];
+  float lsm[C5_BK * C5_BK];  // log2(smask), -inf for zero cells
   double inv_n;            // 1 / (batch * w * h)
   float2 *loss_part;       // per block Kahan (s, c)
   float *dc_part;          // per block
@@ -65,23 +111,19 @@ struct C5Params {
   unsigned int *tickets;   // [0] forward, [1] bilateral adjoint, [2] conv adjoint
   double *loss_dev;
   float *grad_mask_dev, *grad_sigma_dev;
-  int fuse_conv;           // forward computes y1 from x (else reads y1)
-  int fuse_loss;           // forward writes a (else writes y and W into a)
-  int symmetric;           // bilateral adjoint reuses weights
-  int fuse_dmask;          // conv adjoint accumulates dL/dmask
   int img_offset;          // image of the launch (per-image launches; 0 otherwise)
   int tiles_x, tiles_y, ntiles;  // tile grid of the launch (all images, or one image)
-  int combine;             // the launch covers the batch: its last CTA publishes the sums
 };
 
 // tile t of the launch: image, origin
+template <int TW, int TH>
 __device__ __forceinline__ void tile_origin(const C5Params &p, int t, int &b, int &X0, int &Y0) {
   const int per = p.tiles_x * p.tiles_y;
   const int bz = t / per, r = t - bz * per;
   const int by = r / p.tiles_x;
   b = bz + p.img_offset;
-  X0 = (r - by * p.tiles_x) * C5_TW;
-  Y0 = by * C5_TH;
+  X0 = (r - by * p.tiles_x) * TW;
+  Y0 = by * TH;
 }
 
 // Deterministic block-wide FP64 sum of item(0..n-1): thread t folds items
@@ -117,7 +159,7 @@ __device__ __forceinline__ void sigma_consts(const C5Params &p, float &c, float 
   k2 = -c * 1.4426950408889634f;
 }
 
-// block-wide sum of a float (all threads get nothing; thread 0 returns the value)
+// block-wide sum of a float (thread 0 returns the value)
 __device__ __forceinline__ float block_sum_f(float v, float *sbuf) {
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
@@ -130,113 +172,56 @@ __device__ __forceinline__ float block_sum_f(float v, float *sbuf) {
   return r;
 }
 
-// ------------------------------------------------------------------ forward
-__global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant__ C5Params p) {
-  __shared__ float xs[XS_W * XS_H];
-  __shared__ float ys[YS_W * YS_H];
-  __shared__ float msk[C5_MK * C5_MK];
-  __shared__ double dsh[C5_T];
-  const int W = p.w, H = p.h, bm = p.bmode;
-  for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) msk[i] = __ldg(p.mask_dev + i);
-  float c, k2;
-  sigma_consts(p, c, k2);
-  Kahan lsum{0.0f, 0.0f};
-  // persistent: the CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...
-  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
-  int b, X0, Y0;
-  tile_origin(p, tile, b, X0, Y0);
-  const float *x = p.x + (int64_t)b * p.xb;
-  __syncthreads();  // the previous tile's reads of xs / ys are done
-  if (p.fuse_conv) {
-    constexpr int R = C5_MR + C5_BR;
-    for (int c = threadIdx.x; c < XS_W * XS_H; c += C5_T) {
-      const int r = c / XS_W, q = c - r * XS_W;
-      const int ry = remap_c5(bm, Y0 - R + r, H), rx = remap_c5(bm, X0 - R + q, W);
-      xs[c] = (ry == (int)0x80000000 || rx == (int)0x80000000) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
-    }
-    __syncthreads();
-    // y1 on the tile + bilateral halo, four adjacent cells per thread from one
-    // row window of the staged x per mask row (taps row-major, as one cell at a
-    // time); a halo cell outside the image is y1 at the remapped position (the
-    // bilateral reads y1 through the boundary)
-    static_assert(YS_W % 4 == 0 && YS_H * (YS_W / 4) <= C5_T, "one group of four cells per thread");
-    for (int g = threadIdx.x; g < YS_H * (YS_W / 4); g += C5_T) {
-      const int r = g / (YS_W / 4), q4 = (g - r * (YS_W / 4)) * 4;
-      const int vy = Y0 - C5_BR + r, vx = X0 - C5_BR + q4;
-      if (vy >= 0 && vy < H && vx >= 0 && vx + 3 < W) {
-        // staged rows r .. r + 6, columns q4 .. q4 + 9 (R = MR + BR)
-        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int my = 0; my < C5_MK; ++my) {
-          float v[4 + C5_MK - 1];
-#pragma unroll
-          for (int i = 0; i < 4 + C5_MK - 1; ++i) v[i] = xs[(r + my) * XS_W + q4 + i];
-#pragma unroll
-          for (int mx = 0; mx < C5_MK; ++mx)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) acc[j] = __fmaf_rn(msk[my * C5_MK + mx], v[j + mx], acc[j]);
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) ys[r * YS_W + q4 + j] = acc[j];
-        continue;
-      }
-      for (int j = 0; j < 4; ++j) {
-        const int ry = remap_c5(bm, vy, H), rx = remap_c5(bm, vx + j, W);
-        float acc = 0.0f;
-        if (ry != (int)0x80000000 && rx != (int)0x80000000) {
-          // staged x coordinate of (ry - 3, rx - 3)
-          const int sy = ry - C5_MR - (Y0 - R), sx = rx - C5_MR - (X0 - R);
-#pragma unroll
-          for (int my = 0; my < C5_MK; ++my)
-#pragma unroll
-            for (int mx = 0; mx < C5_MK; ++mx)
-              acc = __fmaf_rn(msk[my * C5_MK + mx], xs[(sy + my) * XS_W + sx + mx], acc);
-        }
-        ys[r * YS_W + q4 + j] = acc;
-      }
-    }
-  } else {
-    const float *y1 = p.y1 + (int64_t)b * p.ib;
-    for (int c = threadIdx.x; c < YS_W * YS_H; c += C5_T) {
-      const int r = c / YS_W, q = c - r * YS_W;
-      const int ry = remap_c5(bm, Y0 - C5_BR + r, H), rx = remap_c5(bm, X0 - C5_BR + q, W);
-      ys[c] = (ry == (int)0x80000000 || rx == (int)0x80000000) ? 0.0f : __ldg(y1 + (int64_t)ry * p.ip + rx);
-    }
+// per-axis pre-images of index j under the remap, among virtual positions
+// within `rad` of the image: at most 1 + rad entries
+__device__ __forceinline__ int preimages(int mode, int j, int n, int rad, int *out) {
+  int k = 0;
+  out[k++] = j;
+  if (mode == HGB_BOUNDARY_CONSTANT || (j >= rad && j < n - rad)) return k;
+  for (int v = -rad; v < 0; ++v)
+    if (remap(mode, v, 0, n) == j) out[k++] = v;
+  for (int v = n; v < n + rad; ++v)
+    if (remap(mode, v, 0, n) == j) out[k++] = v;
+  return k;
+}
+
+// Band of radius R along the edges of a W x H image, as the pixels that the
+// tile paths leave out: rows [0, R) and [H-R, H) whole, then for the rows in
+// between columns [0, 4) and [W-wr, W), wr = W - 4 floor((W - R) / 4) (the
+// tile paths take groups of four columns whose taps all stay inside).
+__host__ __device__ __forceinline__ int band_right(int W, int R) { return W - 4 * ((W - R) / 4); }
+__host__ __device__ __forceinline__ int band_size(int W, int H, int R) {
+  return 2 * R * W + (H - 2 * R) * (4 + band_right(W, R));
+}
+__device__ __forceinline__ void band_pos(int k, int W, int H, int R, int &y, int &x) {
+  if (k < 2 * R * W) {
+    const int yy = k / W;
+    x = k - yy * W;
+    y = yy < R ? yy : H - 2 * R + yy;
+    return;
   }
-  __syncthreads();
-  const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
-  for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
-    const int gx = X0 + tx, gy = Y0 + py;
-    if (gx >= W || gy >= H) continue;
-    const float ctr = ys[(py + C5_BR) * YS_W + tx + C5_BR];
-    float N = 0.0f, Wt = 0.0f;
-#pragma unroll 3
-    for (int oy = 0; oy < C5_BK; ++oy)
-#pragma unroll
-      for (int ox = 0; ox < C5_BK; ++ox) {
-        const float v = ys[(py + oy) * YS_W + tx + ox];
-        const float d = v - ctr;
-        const float wt = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
-        N = __fmaf_rn(wt, v, N);
-        Wt += wt;
-      }
-    const float yv = N / Wt;
-    const int64_t o = (int64_t)b * p.ib + (int64_t)gy * p.ip + gx;
-    if (p.fuse_conv) p.y1[o] = ctr;
-    if (p.fuse_loss) {
-      const float tv = __ldg(p.t + (int64_t)b * p.tb + (int64_t)gy * p.tp + gx);
-      const float e = yv - tv;
-      lsum = kahan_add(lsum, e * e);
-      p.a[o] = (float)(2.0 * (double)e * p.inv_n) / Wt;
-      p.y[o] = yv;
-    } else {
-      p.y[o] = yv;
-      p.a[o] = Wt;  // the unfused chain keeps W and forms a in its own pass
-    }
+  k -= 2 * R * W;
+  const int mid = (H - 2 * R) * 4;
+  if (k < mid) {
+    y = R + (k >> 2);
+    x = k & 3;
+    return;
   }
-  }  // tiles
-  if (!p.fuse_loss) return;
-  // per-CTA Kahan partial of the squared error, FP64 combine by the last CTA
+  k -= mid;
+  const int wr = band_right(W, R);
+  const int yy = k / wr;
+  y = R + yy;
+  x = W - wr + (k - yy * wr);
+}
+
+// the contiguous share of n band entries that this CTA takes
+__device__ __forceinline__ void cta_share(int64_t n, int64_t &k0, int64_t &k1) {
+  k0 = n * blockIdx.x / gridDim.x;
+  k1 = n * (blockIdx.x + 1) / gridDim.x;
+}
+
+// per-CTA Kahan partial of the squared error, FP64 combine by the last CTA
+__device__ __forceinline__ void loss_publish(const C5Params &p, Kahan lsum, double *dsh) {
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) {
     Kahan o;
@@ -268,13 +253,547 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
   }
 }
 
-// unfused chain: a = 2 (y - t) / (n W) and the loss partials, one image
+// ================================================================== fused form
+
+// one bilateral tap for a pixel pair: weight e = exp2(-(d'^2 + nl))
+__device__ __forceinline__ void bil_tap(f2 V, f2 C, f2 NL, f2 &Ws, f2 &Ns) {
+  const f2 d = f2_sub(V, C);
+  const f2 t = f2_fma(d, d, NL);
+  const f2 e = f2_pack(ex2f(-f2_lo(t)), ex2f(-f2_hi(t)));
+  Ws = f2_add(Ws, e);
+  Ns = f2_fma(e, V, Ns);
+}
+
+__global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant__ C5Params p) {
+  __shared__ __align__(16) float xs[FX_H * FX_W];
+  __shared__ __align__(16) float us[FY_H * FY_W];
+  __shared__ f2 m2[C5_MK * C5_MK];
+  __shared__ f2 nl2[C5_BK * C5_BK];
+  __shared__ double dsh[C5_T];
+  const int W = p.w, H = p.h, bm = p.bmode;
+  for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) {
+    const float m = __ldg(p.mask_dev + i);
+    m2[i] = f2_pack(m, m);
+  }
+  for (int i = threadIdx.x; i < C5_BK * C5_BK; i += C5_T) nl2[i] = f2_pack(-p.lsm[i], -p.lsm[i]);
+  float c, k2;
+  sigma_consts(p, c, k2);
+  const float q = sqrtf(-k2), inv_q = 1.0f / q;
+  const float g_scale = (float)(2.0 * p.inv_n);
+  const int tx = threadIdx.x % F_GX, ty = threadIdx.x / F_GX;
+  Kahan lsum{0.0f, 0.0f};
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+    int b, X0, Y0;
+    tile_origin<F_TW, F_TH>(p, tile, b, X0, Y0);
+    const float *x = p.x + (int64_t)b * p.xb;
+    __syncthreads();  // the previous tile's reads of xs / us are done
+    // x on rows Y0-7 .., columns X0-8 .. through the boundary
+    if (p.vec_x && X0 >= 8 && X0 + F_TW + 8 <= W && Y0 >= FX_R && Y0 + F_TH + FX_R <= H) {
+      for (int c4 = threadIdx.x; c4 < FX_H * (FX_W / 4); c4 += C5_T) {
+        const int r = c4 / (FX_W / 4), k4 = c4 - r * (FX_W / 4);
+        reinterpret_cast<float4 *>(xs)[c4] =
+            __ldg(reinterpret_cast<const float4 *>(x + (int64_t)(Y0 - FX_R + r) * p.xp + X0 - 8) + k4);
+      }
+    } else {
+      for (int cc = threadIdx.x; cc < FX_H * FX_W; cc += C5_T) {
+        const int r = cc / FX_W, k = cc - r * FX_W;
+        const int ry = remap_c5(bm, Y0 - FX_R + r, H), rx = remap_c5(bm, X0 - 8 + k, W);
+        xs[cc] = (ry == C5_OUT || rx == C5_OUT) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
+      }
+    }
+    __syncthreads();
+    // u = q y1 on rows Y0-4 .., columns X0-4 ..: eight cells per thread from
+    // one 16-value row window of x per mask row, taps row-major (y1 exactly as
+    // hgb_local_op computes it)
+    if (threadIdx.x < FY_H * (FY_W / 8)) {
+      const int r = threadIdx.x / (FY_W / 8), k0 = (threadIdx.x - r * (FY_W / 8)) * 8;
+      f2 acc[4] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll
+      for (int my = 0; my < C5_MK; ++my) {
+        const float4 *row = reinterpret_cast<const float4 *>(&xs[(r + my) * FX_W + k0]);
+        float w[16];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const float4 t4 = row[v];
+          w[4 * v] = t4.x;
+          w[4 * v + 1] = t4.y;
+          w[4 * v + 2] = t4.z;
+          w[4 * v + 3] = t4.w;
+        }
+#pragma unroll
+        for (int mx = 0; mx < C5_MK; ++mx) {
+          const f2 M = m2[my * C5_MK + mx];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) acc[i] = f2_fma(M, f2_pack(w[2 * i + 1 + mx], w[2 * i + 2 + mx]), acc[i]);
+        }
+      }
+      float4 *o = reinterpret_cast<float4 *>(&us[r * FY_W + k0]);
+      o[0] = make_float4(q * f2_lo(acc[0]), q * f2_hi(acc[0]), q * f2_lo(acc[1]), q * f2_hi(acc[1]));
+      o[1] = make_float4(q * f2_lo(acc[2]), q * f2_hi(acc[2]), q * f2_lo(acc[3]), q * f2_hi(acc[3]));
+    }
+    __syncthreads();
+    // a cell outside the image is u at the remapped position (the bilateral
+    // reads y1 through the boundary); cells beyond the radius of the image
+    // are read by no pixel of it
+    if (!(X0 >= C5_BR && X0 + F_TW + C5_BR <= W && Y0 >= C5_BR && Y0 + F_TH + C5_BR <= H)) {
+      for (int cc = threadIdx.x; cc < FY_H * FY_W; cc += C5_T) {
+        const int r = cc / FY_W, k = cc - r * FY_W;
+        const int vy = Y0 - C5_BR + r, vx = X0 - C5_BR + k;
+        if (vy >= 0 && vy < H && vx >= 0 && vx < W) continue;
+        if (vy < -C5_BR || vy >= H + C5_BR || vx < -C5_BR || vx >= W + C5_BR) continue;
+        const int ry = remap_c5(bm, vy, H), rx = remap_c5(bm, vx, W);
+        us[cc] = (ry == C5_OUT || rx == C5_OUT) ? 0.0f : us[(ry - Y0 + C5_BR) * FY_W + rx - X0 + C5_BR];
+      }
+      __syncthreads();
+    }
+    // bilateral: pixels 4 tx .. 4 tx + 3 of row ty, pairs (0, 1) and (2, 3)
+    const float4 cv = *reinterpret_cast<const float4 *>(&us[(ty + C5_BR) * FY_W + 4 * tx + C5_BR]);
+    const f2 C0 = f2_pack(cv.x, cv.y), C1 = f2_pack(cv.z, cv.w);
+    f2 Ws0 = 0ull, Ws1 = 0ull, Ns0 = 0ull, Ns1 = 0ull;
+#pragma unroll 1
+    for (int oy = 0; oy < C5_BK; ++oy) {
+      const float4 *row = reinterpret_cast<const float4 *>(&us[(ty + oy) * FY_W + 4 * tx]);
+      float w[12];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        const float4 t4 = row[v];
+        w[4 * v] = t4.x;
+        w[4 * v + 1] = t4.y;
+        w[4 * v + 2] = t4.z;
+        w[4 * v + 3] = t4.w;
+      }
+#pragma unroll
+      for (int ox = 0; ox < C5_BK; ++ox) {
+        const f2 NL = nl2[oy * C5_BK + ox];
+        bil_tap(f2_pack(w[ox], w[ox + 1]), C0, NL, Ws0, Ns0);
+        bil_tap(f2_pack(w[ox + 2], w[ox + 3]), C1, NL, Ws1, Ns1);
+      }
+    }
+    const int gy = Y0 + ty, gx0 = X0 + 4 * tx;
+    if (gy < H && gx0 < W) {
+      const float Wv[4] = {f2_lo(Ws0), f2_hi(Ws0), f2_lo(Ws1), f2_hi(Ws1)};
+      const float Nv[4] = {f2_lo(Ns0), f2_hi(Ns0), f2_lo(Ns1), f2_hi(Ns1)};
+      const float Uv[4] = {cv.x, cv.y, cv.z, cv.w};
+      const float *trow = p.t + (int64_t)b * p.tb + (int64_t)gy * p.tp;
+      float4 *orow = p.pk + (int64_t)b * p.ib + (int64_t)gy * p.ip;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int gx = gx0 + i;
+        if (gx >= W) break;
+        const float uy = Nv[i] / Wv[i];
+        const float e = uy * inv_q - __ldg(trow + gx);
+        lsum = kahan_add(lsum, e * e);
+        const float a = (g_scale * e) / Wv[i];
+        orow[gx] = make_float4(Uv[i], a, -a * uy, uy);
+      }
+    }
+  }  // tiles
+  loss_publish(p, lsum, dsh);
+}
+
+// one symmetric tap of the bilateral adjoint for a pixel pair j (centre U, A =
+// a_j, B = -a_j u_yj) and its neighbour pair p = j - o (Pu, Pa, PB = -a_p
+// u_yp); s = {sum e a_p, sum e d (u_j a_p - a_p u_yp), sum e d a_j (u_p -
+// u_yj), the same times d} with d = u_j - u_p
+__device__ __forceinline__ void adj_tap(f2 Pu, f2 Pa, f2 PB, f2 U, f2 A, f2 B, f2 NL, f2 (&s)[4]) {
+  const f2 d = f2_sub(U, Pu);
+  const f2 t = f2_fma(d, d, NL);
+  const f2 e = f2_pack(ex2f(-f2_lo(t)), ex2f(-f2_hi(t)));
+  const f2 h = f2_mul(e, d);
+  s[0] = f2_fma(e, Pa, s[0]);
+  s[1] = f2_fma(h, f2_fma(U, Pa, PB), s[1]);
+  const f2 wd = f2_mul(h, f2_fma(A, Pu, B));
+  s[2] = f2_add(s[2], wd);
+  s[3] = f2_fma(wd, d, s[3]);
+}
+
+// dL/dy1 of a band pixel j through the pre-images, from the forward's packed
+// values; adds j's dL/dc share (times -q^3) to dc
+__device__ float bil_adj_band(const C5Params &p, const float4 *pk, int jy, int jx, const float *lsm, float inv_q3,
+                              float &dc) {
+  const int W = p.w, H = p.h, bm = p.bmode;
+  const float4 J = __ldg(pk + (int64_t)jy * p.ip + jx);
+  // centre term and dL/dc over j's own taps, read through the boundary
+  int rx[C5_BK];
+#pragma unroll
+  for (int o = 0; o < C5_BK; ++o) rx[o] = remap_c5(bm, jx + o - C5_BR, W);
+  float ctr = 0.0f, s2 = 0.0f;
+  for (int oy = 0; oy < C5_BK; ++oy) {
+    const int ry = remap_c5(bm, jy + oy - C5_BR, H);
+#pragma unroll
+    for (int ox = 0; ox < C5_BK; ++ox) {
+      const float uq = (ry == C5_OUT || rx[ox] == C5_OUT) ? 0.0f : __ldg(pk + (int64_t)ry * p.ip + rx[ox]).x;
+      const float d = uq - J.x;
+      const float e = ex2f(__fmaf_rn(-d, d, lsm[oy * C5_BK + ox]));
+      const float wd = e * __fmaf_rn(J.y, uq, J.z) * d;
+      ctr += wd;
+      s2 = __fmaf_rn(wd, d, s2);
+    }
+  }
+  dc = __fmaf_rn(-inv_q3, s2, dc);
+  // neighbour term gathered over the pre-images of j
+  int prx[1 + C5_BR], pry[1 + C5_BR];
+  const int nx = preimages(bm, jx, W, C5_BR, prx), ny = preimages(bm, jy, H, C5_BR, pry);
+  float dn = 0.0f;
+  for (int iy = 0; iy < ny; ++iy)
+    for (int oy = 0; oy < C5_BK; ++oy) {
+      const int py = pry[iy] - (oy - C5_BR);
+      if (py < 0 || py >= H) continue;
+      for (int ix = 0; ix < nx; ++ix)
+        for (int ox = 0; ox < C5_BK; ++ox) {
+          const int px = prx[ix] - (ox - C5_BR);
+          if (px < 0 || px >= W) continue;
+          const float4 P = __ldg(pk + (int64_t)py * p.ip + px);
+          const float d = J.x - P.x;
+          const float e = ex2f(__fmaf_rn(-d, d, lsm[oy * C5_BK + ox]));
+          dn = __fmaf_rn(e, __fmaf_rn(-C2S * d, __fmaf_rn(J.x, P.y, P.z), P.y), dn);
+        }
+    }
+  return __fmaf_rn(C2S, ctr, dn);
+}
+
+__global__ void __launch_bounds__(C5_T, 4) c5_bilateral_adjoint_kernel(const __grid_constant__ C5Params p) {
+  // per staged position k of a row: (u_k, u_k+1, a_k, a_k+1) and (B_k, B_k+1),
+  // so that a pixel pair's neighbours at any offset are one aligned load each
+  __shared__ __align__(16) float4 sq[FY_H * SQ_W];
+  __shared__ __align__(16) f2 sb[FY_H * SB_W];
+  __shared__ f2 nl2[C5_BK * C5_BK];
+  __shared__ float lsm[C5_BK * C5_BK];
+  __shared__ float sbuf[32];
+  double *dsh = reinterpret_cast<double *>(sq);  // the final combine, after the tiles
+  const int W = p.w, H = p.h;
+  for (int i = threadIdx.x; i < C5_BK * C5_BK; i += C5_T) {
+    lsm[i] = p.lsm[i];
+    nl2[i] = f2_pack(-p.lsm[i], -p.lsm[i]);
+  }
+  float c, k2;
+  sigma_consts(p, c, k2);
+  const float q = sqrtf(-k2), inv_q = 1.0f / q;
+  const float inv_q3 = inv_q * inv_q * inv_q;
+  const int tx = threadIdx.x % F_GX, ty = threadIdx.x / F_GX;
+  float dc = 0.0f;
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+    int b, X0, Y0;
+    tile_origin<F_TW, F_TH>(p, tile, b, X0, Y0);
+    const float4 *pk = p.pk + (int64_t)b * p.ib;
+    __syncthreads();  // the previous tile's reads are done
+    // in-image cells of rows Y0-4 .., columns X0-4 ..: two positions per item
+    for (int it = threadIdx.x; it < FY_H * (FY_W / 2); it += C5_T) {
+      const int r = it / (FY_W / 2), k = (it - r * (FY_W / 2)) * 2;
+      const int gy = Y0 - C5_BR + r, gx = X0 - C5_BR + k;
+      if (gy < 0 || gy >= H) continue;
+      const float4 *src = pk + (int64_t)gy * p.ip;
+      const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const float4 v0 = (gx >= 0 && gx < W) ? __ldg(src + gx) : z;
+      const float4 v1 = (gx + 1 >= 0 && gx + 1 < W) ? __ldg(src + gx + 1) : z;
+      const float4 v2 = (gx + 2 >= 0 && gx + 2 < W) ? __ldg(src + gx + 2) : z;
+      sq[r * SQ_W + skew8(k)] = make_float4(v0.x, v1.x, v0.y, v1.y);
+      sq[r * SQ_W + skew8(k + 1)] = make_float4(v1.x, v2.x, v1.y, v2.y);
+      sb[r * SB_W + skew16(k)] = f2_pack(v0.z, v1.z);
+      sb[r * SB_W + skew16(k + 1)] = f2_pack(v1.z, v2.z);
+    }
+    __syncthreads();
+    const int jx0 = X0 + 4 * tx, jy = Y0 + ty;
+    if (jx0 >= C5_BR && jx0 + 3 < W - C5_BR && jy >= C5_BR && jy < H - C5_BR) {
+      // skewed position 4 tx + s of a row = base + s + (s < 4 ? 0 : s < 8 ? k1 : k2)
+      const int q1 = tx & 1, b1 = (tx & 3) == 3, b2 = (tx & 3) >= 2;
+      const int qbase = 4 * tx + (tx >> 1), bbase = 4 * tx + (tx >> 2);
+      const int ce_q = (ty + C5_BR) * SQ_W + qbase + q1, ce_b = (ty + C5_BR) * SB_W + bbase + b1;
+      const float4 J0 = sq[ce_q + 4], J1 = sq[ce_q + 6];
+      const f2 U0 = f2_pack(J0.x, J0.y), U1 = f2_pack(J1.x, J1.y);
+      const f2 A0 = f2_pack(J0.z, J0.w), A1 = f2_pack(J1.z, J1.w);
+      const f2 B0 = sb[ce_b + 4], B1 = sb[ce_b + 6];
+      f2 s0[4] = {0ull, 0ull, 0ull, 0ull}, s1[4] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll 1
+      for (int oy = 0; oy < C5_BK; ++oy) {
+        // neighbours p = j - o: row ty + 8 - oy, positions 4 tx + s, s = 0 .. 10;
+        // pair 0 takes tap ox = 8 - s, pair 1 tap ox = 10 - s
+        const int row = ty + 2 * C5_BR - oy;
+        const float4 *qr = &sq[row * SQ_W + qbase];
+        const f2 *br = &sb[row * SB_W + bbase];
+        f2 NL[C5_BK];
+#pragma unroll
+        for (int ox = 0; ox < C5_BK; ++ox) NL[ox] = nl2[oy * C5_BK + ox];
+#pragma unroll
+        for (int s = 0; s <= 2 * C5_BR + 2; ++s) {
+          const float4 P = qr[s + (s < 4 ? 0 : s < 8 ? q1 : 1)];
+          const f2 Pu = f2_pack(P.x, P.y), Pa = f2_pack(P.z, P.w), PB = br[s + (s < 4 ? 0 : s < 8 ? b1 : b2)];
+          if (s <= 2 * C5_BR) adj_tap(Pu, Pa, PB, U0, A0, B0, NL[2 * C5_BR - s], s0);
+          if (s >= 2) adj_tap(Pu, Pa, PB, U1, A1, B1, NL[2 * C5_BR + 2 - s], s1);
+        }
+      }
+      // dL/dy1 = sum e a_p - C2S (neighbour sum + centre sum); dL/dc share -s3 / q^3
+      const float4 o = make_float4(f2_lo(s0[0]) - C2S * (f2_lo(s0[1]) + f2_lo(s0[2])),
+                                   f2_hi(s0[0]) - C2S * (f2_hi(s0[1]) + f2_hi(s0[2])),
+                                   f2_lo(s1[0]) - C2S * (f2_lo(s1[1]) + f2_lo(s1[2])),
+                                   f2_hi(s1[0]) - C2S * (f2_hi(s1[1]) + f2_hi(s1[2])));
+      *reinterpret_cast<float4 *>(p.dy1 + (int64_t)b * p.ib + (int64_t)jy * p.ip + jx0) = o;
+      dc = __fmaf_rn(-inv_q3, (f2_lo(s0[3]) + f2_hi(s0[3])) + (f2_lo(s1[3]) + f2_hi(s1[3])), dc);
+    }
+  }  // tiles
+  // band pixels of every image of the batch: an equal contiguous share per CTA
+  {
+    const int per = band_size(W, H, C5_BR);
+    int64_t k0, k1;
+    cta_share((int64_t)per * p.batch, k0, k1);
+    for (int64_t k = k0 + threadIdx.x; k < k1; k += C5_T) {
+      const int b = (int)(k / per);
+      int jy, jx;
+      band_pos((int)(k - (int64_t)b * per), W, H, C5_BR, jy, jx);
+      const float g = bil_adj_band(p, p.pk + (int64_t)b * p.ib, jy, jx, lsm, inv_q3, dc);
+      p.dy1[(int64_t)b * p.ib + (int64_t)jy * p.ip + jx] = g;
+    }
+  }
+  const float bdc = block_sum_f(dc, sbuf);
+  const unsigned int nb = grid_blocks();
+  if (threadIdx.x == 0) p.dc_part[block_rank()] = bdc;
+  if (take_last_ticket(p.tickets + 1)) {
+    const double s = block_sum_fixed((int)nb, [&](int i) { return (double)__ldcg(p.dc_part + i); }, dsh);
+    if (threadIdx.x == 0) {
+      const double sg = (double)__ldg(p.sigma_dev);
+      *p.grad_sigma_dev = (float)(s * (-1.0 / (sg * sg * sg)));
+      p.tickets[1] = 0u;
+    }
+  }
+}
+
+// stage one row segment of four positions k .. k+3 (k a multiple of 4, so the
+// skewed positions are consecutive) as pairs (v_k, v_k+1): in-image values,
+// zero elsewhere
+__device__ __forceinline__ void stage_pairs4(f2 *dst, const float *row, int gx, int W, bool vec) {
+  float v[5];
+  if (vec && gx >= 0 && gx + 4 < W) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(row + gx));
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = a.z;
+    v[3] = a.w;
+    v[4] = __ldg(row + gx + 4);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) v[i] = (gx + i >= 0 && gx + i < W) ? __ldg(row + gx + i) : 0.0f;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) dst[i] = f2_pack(v[i], v[i + 1]);
+}
+
+__global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_constant__ C5Params p) {
+  __shared__ __align__(16) f2 sg[FC_H * SC_W];  // (dy1_k, dy1_k+1)
+  __shared__ __align__(16) f2 sx[FC_H * SC_W];  // (x_k, x_k+1)
+  __shared__ f2 m2[C5_MK * C5_MK];
+  __shared__ float msk[C5_MK * C5_MK];
+  __shared__ float red[C5_T / 32][C5_MK * C5_MK];
+  __shared__ double dsh[C5_T];
+  const int W = p.w, H = p.h, bm = p.bmode;
+  for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) {
+    const float m = __ldg(p.mask_dev + i);
+    msk[i] = m;
+    m2[i] = f2_pack(m, m);
+  }
+  // band pixels of every image of the batch, an equal contiguous share per
+  // CTA; first part (before the mask-gradient registers are live): grad_in
+  // through the pre-images
+  const int band_per = band_size(W, H, C5_MR);
+  int64_t k0, k1;
+  cta_share((int64_t)band_per * p.batch, k0, k1);
+  __syncthreads();  // msk
+  for (int64_t k = k0 + threadIdx.x; k < k1; k += C5_T) {
+    const int b = (int)(k / band_per);
+    int jy, jx;
+    band_pos((int)(k - (int64_t)b * band_per), W, H, C5_MR, jy, jx);
+    const float *g = p.dy1 + (int64_t)b * p.ib;
+    // grad_in through the pre-images of j
+    int prx[1 + C5_MR], pry[1 + C5_MR];
+    const int nx = preimages(bm, jx, W, C5_MR, prx), ny = preimages(bm, jy, H, C5_MR, pry);
+    float acc = 0.0f;
+    for (int iy = 0; iy < ny; ++iy)
+      for (int oy = 0; oy < C5_MK; ++oy) {
+        const int sy = pry[iy] - (oy - C5_MR);
+        if (sy < 0 || sy >= H) continue;
+        for (int ix = 0; ix < nx; ++ix)
+          for (int ox = 0; ox < C5_MK; ++ox) {
+            const int sxp = prx[ix] - (ox - C5_MR);
+            if (sxp < 0 || sxp >= W) continue;
+            acc = __fmaf_rn(msk[oy * C5_MK + ox], g[(int64_t)sy * p.ip + sxp], acc);
+          }
+      }
+    p.dx[(int64_t)b * p.dxb + (int64_t)jy * p.dxp + jx] = acc;
+  }
+  const int tx = threadIdx.x % F_GX, ty = threadIdx.x / F_GX;
+  // dL/dmask per pair of taps (oy, 2 op), (oy, 2 op + 1); the eighth tap of a
+  // row is padding
+  f2 DM[C5_MK][4];
+#pragma unroll
+  for (int i = 0; i < C5_MK; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) DM[i][j] = 0ull;
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+    int b, X0, Y0;
+    tile_origin<F_TW, F_TH>(p, tile, b, X0, Y0);
+    const float *g = p.dy1 + (int64_t)b * p.ib;
+    const float *x = p.x + (int64_t)b * p.xb;
+    __syncthreads();  // the previous tile's reads are done
+    // rows Y0-3 .., columns X0-4 ..: four positions per item
+    for (int it = threadIdx.x; it < FC_H * (FC_W / 4); it += C5_T) {
+      const int r = it / (FC_W / 4), k = (it - r * (FC_W / 4)) * 4;
+      const int gy = Y0 - C5_MR + r, gx = X0 - 4 + k;
+      if (gy < 0 || gy >= H) continue;
+      stage_pairs4(&sg[r * SC_W + skew16(k)], g + (int64_t)gy * p.ip, gx, W, true);
+      stage_pairs4(&sx[r * SC_W + skew16(k)], x + (int64_t)gy * p.xp, gx, W, p.vec_x);
+    }
+    __syncthreads();
+    const int jx0 = X0 + 4 * tx, jy = Y0 + ty;
+    if (jx0 >= 4 && jx0 + 3 < W - C5_MR && jy >= C5_MR && jy < H - C5_MR) {
+      // skewed position 4 tx + s of a row = base + s + (s < 4 ? 0 : s < 8 ? k1 : k2)
+      const int b1 = (tx & 3) == 3, b2 = (tx & 3) >= 2, base = 4 * tx + (tx >> 2);
+      auto at = [&](const f2 *row, int s) { return row[s + (s < 4 ? 0 : s < 8 ? b1 : b2)]; };
+      // grad_in: pixel pair pp at position 4 tx + 4 + 2 pp gathers dy1 at
+      // positions 4 tx + 7 + 2 pp - ox of row ty + 6 - oy
+      f2 GI0 = 0ull, GI1 = 0ull;
+#pragma unroll
+      for (int oy = 0; oy < C5_MK; ++oy) {
+        const f2 *row = &sg[(ty + 2 * C5_MR - oy) * SC_W + base];
+        f2 gw[9];
+#pragma unroll
+        for (int s = 0; s < 9; ++s) gw[s] = at(row, s + 1);
+#pragma unroll
+        for (int ox = 0; ox < C5_MK; ++ox) {
+          const f2 M = m2[oy * C5_MK + ox];
+          GI0 = f2_fma(M, gw[6 - ox], GI0);
+          GI1 = f2_fma(M, gw[8 - ox], GI1);
+        }
+      }
+      float *dxr = p.dx + (int64_t)b * p.dxb + (int64_t)jy * p.dxp + jx0;
+      if (p.vec_dx) {
+        *reinterpret_cast<float4 *>(dxr) = make_float4(f2_lo(GI0), f2_hi(GI0), f2_lo(GI1), f2_hi(GI1));
+      } else {
+        dxr[0] = f2_lo(GI0);
+        dxr[1] = f2_hi(GI0);
+        dxr[2] = f2_lo(GI1);
+        dxr[3] = f2_hi(GI1);
+      }
+      // mask gradient: pixel i (position 4 tx + 4 + i) with x at positions
+      // 4 tx + 1 + i + ox of row ty + oy
+      const f2 gc0 = at(&sg[(ty + C5_MR) * SC_W + base], 4), gc1 = at(&sg[(ty + C5_MR) * SC_W + base], 6);
+      const f2 GG[4] = {f2_pack(f2_lo(gc0), f2_lo(gc0)), f2_pack(f2_hi(gc0), f2_hi(gc0)),
+                        f2_pack(f2_lo(gc1), f2_lo(gc1)), f2_pack(f2_hi(gc1), f2_hi(gc1))};
+#pragma unroll
+      for (int oy = 0; oy < C5_MK; ++oy) {
+        const f2 *row = &sx[(ty + oy) * SC_W + base];
+        f2 xw[12];
+#pragma unroll
+        for (int s = 0; s < 12; ++s) xw[s] = at(row, s);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int op = 0; op < 4; ++op) DM[oy][op] = f2_fma(GG[i], xw[1 + i + 2 * op], DM[oy][op]);
+      }
+    }
+  }  // tiles
+  // band pixels, second part: their mask-gradient terms
+  for (int64_t k = k0 + threadIdx.x; k < k1; k += C5_T) {
+    const int b = (int)(k / band_per);
+    int jy, jx;
+    band_pos((int)(k - (int64_t)b * band_per), W, H, C5_MR, jy, jx);
+    const float *g = p.dy1 + (int64_t)b * p.ib;
+    const float *x = p.x + (int64_t)b * p.xb;
+    // mask gradient with x through the boundary (CONSTANT taps outside carry none)
+    const float gj = g[(int64_t)jy * p.ip + jx];
+    const f2 GJ = f2_pack(gj, gj);
+    int rx[2 * 4];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) rx[o] = o < C5_MK ? remap_c5(bm, jx + o - C5_MR, W) : C5_OUT;
+#pragma unroll
+    for (int oy = 0; oy < C5_MK; ++oy) {
+      const int ry = remap_c5(bm, jy + oy - C5_MR, H);
+#pragma unroll
+      for (int op = 0; op < 4; ++op) {
+        const float x0 =
+            (ry == C5_OUT || rx[2 * op] == C5_OUT) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx[2 * op]);
+        const float x1 =
+            (ry == C5_OUT || rx[2 * op + 1] == C5_OUT) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx[2 * op + 1]);
+        DM[oy][op] = f2_fma(GJ, f2_pack(x0, x1), DM[oy][op]);
+      }
+    }
+  }
+  // block partials of dL/dmask (49 values), FP64 combine by the last block
+#pragma unroll
+  for (int oy = 0; oy < C5_MK; ++oy)
+#pragma unroll
+    for (int ox = 0; ox < C5_MK; ++ox) {
+      float v = (ox & 1) ? f2_hi(DM[oy][ox >> 1]) : f2_lo(DM[oy][ox >> 1]);
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][oy * C5_MK + ox] = v;
+    }
+  __syncthreads();
+  const unsigned int nb = grid_blocks();
+  if (threadIdx.x < C5_MK * C5_MK) {
+    float s = 0.0f;
+    for (int wv = 0; wv < C5_T / 32; ++wv) s += red[wv][threadIdx.x];
+    p.dm_part[(size_t)block_rank() * C5_MK * C5_MK + threadIdx.x] = s;
+    __threadfence();
+  }
+  if (take_last_ticket(p.tickets + 2)) {
+    for (int o = 0; o < C5_MK * C5_MK; ++o) {
+      const double s = block_sum_fixed(
+          (int)nb, [&](int i) { return (double)__ldcg(p.dm_part + (size_t)i * C5_MK * C5_MK + o); }, dsh);
+      if (threadIdx.x == 0) p.grad_mask_dev[o] = (float)s;
+    }
+    if (threadIdx.x == 0) p.tickets[2] = 0u;
+  }
+}
+
+// ================================================================== unfused form
+
+// bilateral forward of one image from y1 (computed by hgb_local_op): writes y
+// and W (into a); the loss gradient follows in its own pass
+__global__ void __launch_bounds__(C5_T) c5u_forward_kernel(const __grid_constant__ C5Params p) {
+  __shared__ float ys[UY_W * UY_H];
+  const int W = p.w, H = p.h, bm = p.bmode;
+  float c, k2;
+  sigma_consts(p, c, k2);
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+    int b, X0, Y0;
+    tile_origin<U_TW, U_TH>(p, tile, b, X0, Y0);
+    const float *y1 = p.y1 + (int64_t)b * p.ib;
+    __syncthreads();  // the previous tile's reads of ys are done
+    for (int cc = threadIdx.x; cc < UY_W * UY_H; cc += C5_T) {
+      const int r = cc / UY_W, k = cc - r * UY_W;
+      const int ry = remap_c5(bm, Y0 - C5_BR + r, H), rx = remap_c5(bm, X0 - C5_BR + k, W);
+      ys[cc] = (ry == C5_OUT || rx == C5_OUT) ? 0.0f : __ldg(y1 + (int64_t)ry * p.ip + rx);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % U_TW, ty = threadIdx.x / U_TW;
+    for (int py = ty; py < U_TH; py += C5_T / U_TW) {
+      const int gx = X0 + tx, gy = Y0 + py;
+      if (gx >= W || gy >= H) continue;
+      const float ctr = ys[(py + C5_BR) * UY_W + tx + C5_BR];
+      float N = 0.0f, Wt = 0.0f;
+#pragma unroll 3
+      for (int oy = 0; oy < C5_BK; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < C5_BK; ++ox) {
+          const float v = ys[(py + oy) * UY_W + tx + ox];
+          const float d = v - ctr;
+          const float wt = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
+          N = __fmaf_rn(wt, v, N);
+          Wt += wt;
+        }
+      const int64_t o = (int64_t)b * p.ib + (int64_t)gy * p.ip + gx;
+      p.y[o] = N / Wt;
+      p.a[o] = Wt;
+    }
+  }
+}
+
+// a = 2 (y - t) / (n W) and the loss partials, one image
 __global__ void __launch_bounds__(C5_T) c5_alpha_kernel(const __grid_constant__ C5Params p) {
   const int b = blockIdx.z + p.img_offset;
-  const int gx = blockIdx.x * C5_TW + threadIdx.x % C5_TW;
+  const int gx = blockIdx.x * U_TW + threadIdx.x % U_TW;
   Kahan lsum{0.0f, 0.0f};
-  for (int py = threadIdx.x / C5_TW; py < C5_TH; py += C5_T / C5_TW) {
-    const int gy = blockIdx.y * C5_TH + py;
+  for (int py = threadIdx.x / U_TW; py < U_TH; py += C5_T / U_TW) {
+    const int gy = blockIdx.y * U_TH + py;
     if (gx >= p.w || gy >= p.h) continue;
     const int64_t o = (int64_t)b * p.ib + (int64_t)gy * p.ip + gx;
     const float e = p.y[o] - __ldg(p.t + (int64_t)b * p.tb + (int64_t)gy * p.tp + gx);
@@ -286,255 +805,113 @@ __global__ void __launch_bounds__(C5_T) c5_alpha_kernel(const __grid_constant__ 
   if (threadIdx.x == 0) p.loss_part[block_rank() + (unsigned)p.img_offset * grid_blocks()] = make_float2(v, 0.0f);
 }
 
-// ------------------------------------------------------------------ bilateral adjoint
-// per-axis pre-images of index j under the remap, among virtual positions
-// within `rad` of the image: at most 1 + rad entries
-__device__ __forceinline__ int preimages(int mode, int j, int n, int rad, int *out) {
-  int k = 0;
-  out[k++] = j;
-  if (mode == HGB_BOUNDARY_CONSTANT || (j >= rad && j < n - rad)) return k;
-  for (int v = -rad; v < 0; ++v)
-    if (remap(mode, v, 0, n) == j) out[k++] = v;
-  for (int v = n; v < n + rad; ++v)
-    if (remap(mode, v, 0, n) == j) out[k++] = v;
-  return k;
-}
-
-__global__ void __launch_bounds__(C5_T) c5_bilateral_adjoint_kernel(const __grid_constant__ C5Params p) {
-  // staged per pixel of the tile + radius: (q y1, a, a q y, q y) with
-  // q = sqrt(c log2 e), so that a tap's weight is exp2(lsm - d'^2) for the
-  // scaled difference d' = q (y1_j - y1_p)
-  __shared__ float4 s4[YS_W * YS_H];
+// bilateral adjoint of one image, every pixel through the pre-images (no
+// weight reuse between the centre and the neighbour terms)
+__global__ void __launch_bounds__(C5_T) c5u_bilateral_adjoint_kernel(const __grid_constant__ C5Params p) {
+  __shared__ float y1s[UY_W * UY_H], as[UY_W * UY_H], yss[UY_W * UY_H];
   __shared__ float sbuf[32];
-  __shared__ double dsh[C5_T];
   const int W = p.w, H = p.h, bm = p.bmode;
   float c, k2;
   sigma_consts(p, c, k2);
   const float c2 = 2.0f * c;
-  const float q = sqrtf(-k2), inv_q = 1.0f / q;
-  // 2c (y1_j - y_p)(y1_j - y1_p) = C2S (q y1_j - q y_p) d' with C2S = 2c / q^2 = 2 ln 2
-  constexpr float C2S = 1.3862943611198906f;
-  const float inv_q3 = inv_q * inv_q * inv_q;
   float dc = 0.0f;
   for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
-  int b, X0, Y0;
-  tile_origin(p, tile, b, X0, Y0);
-  const int64_t base = (int64_t)b * p.ib;
-  __syncthreads();  // the previous tile's reads are done
-  // in-image cells of [X0-4, X0+TW+4) x [Y0-4, Y0+TH+4); others are never read
-  for (int cc = threadIdx.x; cc < YS_W * YS_H; cc += C5_T) {
-    const int r = cc / YS_W, qx = cc - r * YS_W;
-    const int gy = Y0 - C5_BR + r, gx = X0 - C5_BR + qx;
-    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-      const int64_t o = base + (int64_t)gy * p.ip + gx;
-      const float a = p.a[o], uy = q * p.y[o];
-      s4[cc] = make_float4(q * p.y1[o], a, a * uy, uy);
-    }
-  }
-  __syncthreads();
-  const int tx = threadIdx.x % C5_TW, ty = threadIdx.x / C5_TW;
-  auto S = [&](int gy, int gx) { return s4[(gy - Y0 + C5_BR) * YS_W + gx - X0 + C5_BR]; };
-  for (int py = ty; py < C5_TH; py += C5_T / C5_TW) {
-    const int jx = X0 + tx, jy = Y0 + py;
-    if (jx >= W || jy >= H) continue;
-    const int sj = (py + C5_BR) * YS_W + tx + C5_BR;
-    const float4 J = s4[sj];
-    const float u1j = J.x, aj = J.y, uyj = J.w;
-    float dn = 0.0f, s1 = 0.0f, s2 = 0.0f;
-    const bool inner = jx >= C5_BR && jx < W - C5_BR && jy >= C5_BR && jy < H - C5_BR;
-    if (inner && p.symmetric) {
-#pragma unroll 3
-      for (int oy = 0; oy < C5_BK; ++oy)
-#pragma unroll
-        for (int ox = 0; ox < C5_BK; ++ox) {
-          // p = j - o; tap o of p reads j, tap -o of j reads p; one weight
-          const float4 P = s4[sj - (oy - C5_BR) * YS_W - (ox - C5_BR)];
-          const float d = u1j - P.x;
-          const float e = ex2f(__fmaf_rn(-d, d, p.lsm[oy * C5_BK + ox]));
-          // neighbour term a_p e (1 - 2c (y1_j - y_p) d)
-          const float t = __fmaf_rn(u1j, P.y, -P.z);
-          dn = __fmaf_rn(e, __fmaf_rn(-C2S * d, t, P.y), dn);
-          // j's own tap -o: e (y1_p - y_j) d' into the centre and dL/dc sums
-          const float wd = e * (P.x - uyj) * d;
-          s1 += wd;
-          s2 = __fmaf_rn(wd, d, s2);
-        }
-      // centre term a_j sum e (y1_p - y_j) 2c (y1_p - y1_j) = -C2S a_j s1;
-      // dL/dc over j's taps: -a_j s2 / q^3
-      dc = __fmaf_rn(-aj * inv_q3, s2, dc);
-      p.dy1[base + (int64_t)jy * p.ip + jx] = __fmaf_rn(-C2S * aj, s1, dn);
-      continue;
-    }
-    const float y1j = u1j * inv_q, yj = uyj * inv_q;
-    float ctr = 0.0f;
-    // centre term and dL/dc over j's own taps
-    for (int oy = 0; oy < C5_BK; ++oy)
-      for (int ox = 0; ox < C5_BK; ++ox) {
-        const int qy = remap_c5(bm, jy + oy - C5_BR, H), qx = remap_c5(bm, jx + ox - C5_BR, W);
-        const float v = (qy == (int)0x80000000 || qx == (int)0x80000000) ? 0.0f : S(qy, qx).x * inv_q;
-        const float d = v - y1j;
-        const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
-        const float u = e * (v - yj);
-        ctr = __fmaf_rn(u, c2 * d, ctr);
-        dc = __fmaf_rn(aj * u, -(d * d), dc);
+    int b, X0, Y0;
+    tile_origin<U_TW, U_TH>(p, tile, b, X0, Y0);
+    const int64_t base = (int64_t)b * p.ib;
+    __syncthreads();  // the previous tile's reads are done
+    // in-image cells of [X0-4, X0+TW+4) x [Y0-4, Y0+TH+4); others are never read
+    for (int cc = threadIdx.x; cc < UY_W * UY_H; cc += C5_T) {
+      const int r = cc / UY_W, k = cc - r * UY_W;
+      const int gy = Y0 - C5_BR + r, gx = X0 - C5_BR + k;
+      if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+        const int64_t o = base + (int64_t)gy * p.ip + gx;
+        y1s[cc] = p.y1[o];
+        as[cc] = p.a[o];
+        yss[cc] = p.y[o];
       }
-    // neighbour term gathered over the pre-images of j
-    int prx[1 + C5_BR], pry[1 + C5_BR];
-    const int nx = preimages(bm, jx, W, C5_BR, prx), ny = preimages(bm, jy, H, C5_BR, pry);
-    for (int iy = 0; iy < ny; ++iy)
-      for (int ix = 0; ix < nx; ++ix)
-        for (int oy = 0; oy < C5_BK; ++oy)
-          for (int ox = 0; ox < C5_BK; ++ox) {
-            const int qy = pry[iy] - (oy - C5_BR), qx = prx[ix] - (ox - C5_BR);
-            if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
-            const float4 P = S(qy, qx);
-            const float y1p = P.x * inv_q, ypp = P.w * inv_q;
-            const float d = y1j - y1p;
-            const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
-            dn = __fmaf_rn(P.y * e, 1.0f - c2 * (y1j - ypp) * d, dn);
-          }
-    p.dy1[base + (int64_t)jy * p.ip + jx] = __fmaf_rn(aj, ctr, dn);
-  }
+    }
+    __syncthreads();
+    auto S = [&](int gy, int gx) { return (gy - Y0 + C5_BR) * UY_W + gx - X0 + C5_BR; };
+    const int tx = threadIdx.x % U_TW, ty = threadIdx.x / U_TW;
+    for (int py = ty; py < U_TH; py += C5_T / U_TW) {
+      const int jx = X0 + tx, jy = Y0 + py;
+      if (jx >= W || jy >= H) continue;
+      const int sj = S(jy, jx);
+      const float y1j = y1s[sj], aj = as[sj], yj = yss[sj];
+      float ctr = 0.0f;
+      // centre term and dL/dc over j's own taps
+      for (int oy = 0; oy < C5_BK; ++oy)
+        for (int ox = 0; ox < C5_BK; ++ox) {
+          const int qy = remap_c5(bm, jy + oy - C5_BR, H), qx = remap_c5(bm, jx + ox - C5_BR, W);
+          const float v = (qy == C5_OUT || qx == C5_OUT) ? 0.0f : y1s[S(qy, qx)];
+          const float d = v - y1j;
+          const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
+          const float u = e * (v - yj);
+          ctr = __fmaf_rn(u, c2 * d, ctr);
+          dc = __fmaf_rn(aj * u, -(d * d), dc);
+        }
+      // neighbour term gathered over the pre-images of j
+      int prx[1 + C5_BR], pry[1 + C5_BR];
+      const int nx = preimages(bm, jx, W, C5_BR, prx), ny = preimages(bm, jy, H, C5_BR, pry);
+      float dn = 0.0f;
+      for (int iy = 0; iy < ny; ++iy)
+        for (int ix = 0; ix < nx; ++ix)
+          for (int oy = 0; oy < C5_BK; ++oy)
+            for (int ox = 0; ox < C5_BK; ++ox) {
+              const int qy = pry[iy] - (oy - C5_BR), qx = prx[ix] - (ox - C5_BR);
+              if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+              const int sp = S(qy, qx);
+              const float d = y1j - y1s[sp];
+              const float e = ex2f(__fmaf_rn(k2 * d, d, p.lsm[oy * C5_BK + ox]));
+              dn = __fmaf_rn(as[sp] * e, 1.0f - c2 * (y1j - yss[sp]) * d, dn);
+            }
+      p.dy1[base + (int64_t)jy * p.ip + jx] = __fmaf_rn(aj, ctr, dn);
+    }
   }  // tiles
   const float bdc = block_sum_f(dc, sbuf);
-  const unsigned int nb = grid_blocks();
-  const unsigned int rank = block_rank() + (unsigned)p.img_offset * nb;
-  if (threadIdx.x == 0) p.dc_part[rank] = bdc;
-  if (p.combine && take_last_ticket(p.tickets + 1)) {
-    const double s = block_sum_fixed((int)nb, [&](int i) { return (double)__ldcg(p.dc_part + i); }, dsh);
-    if (threadIdx.x == 0) {
-      const double sg = (double)__ldg(p.sigma_dev);
-      *p.grad_sigma_dev = (float)(s * (-1.0 / (sg * sg * sg)));
-      p.tickets[1] = 0u;
-    }
-  }
+  if (threadIdx.x == 0) p.dc_part[block_rank() + (unsigned)p.img_offset * grid_blocks()] = bdc;
 }
 
-// ------------------------------------------------------------------ conv adjoint
-__global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_constant__ C5Params p) {
-  __shared__ float sd[DS_W * DS_H], sx[DS_W * DS_H];
+// convolution adjoint of one image (grad_in only), every pixel through the
+// pre-images
+__global__ void __launch_bounds__(C5_T) c5u_conv_adjoint_kernel(const __grid_constant__ C5Params p) {
+  __shared__ float sd[UD_W * UD_H];
   __shared__ float msk[C5_MK * C5_MK];
-  __shared__ float red[C5_T / 32][C5_MK * C5_MK];
-  __shared__ double dsh[C5_T];
   const int W = p.w, H = p.h, bm = p.bmode;
   for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) msk[i] = __ldg(p.mask_dev + i);
-  float dm[C5_MK * C5_MK];
-#pragma unroll
-  for (int i = 0; i < C5_MK * C5_MK; ++i) dm[i] = 0.0f;
   for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
-  int b, X0, Y0;
-  tile_origin(p, tile, b, X0, Y0);
-  const int64_t base = (int64_t)b * p.ib;
-  const float *x = p.x + (int64_t)b * p.xb;
-  __syncthreads();  // the previous tile's reads are done
-  for (int c = threadIdx.x; c < DS_W * DS_H; c += C5_T) {
-    const int r = c / DS_W, q = c - r * DS_W;
-    const int gy = Y0 - C5_MR + r, gx = X0 - C5_MR + q;
-    sd[c] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? p.dy1[base + (int64_t)gy * p.ip + gx] : 0.0f;
-    const int ry = remap_c5(bm, gy, H), rx = remap_c5(bm, gx, W);
-    sx[c] = (ry == (int)0x80000000 || rx == (int)0x80000000) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
-  }
-  __syncthreads();
-  auto D = [&](int gy, int gx) { return sd[(gy - Y0 + C5_MR) * DS_W + gx - X0 + C5_MR]; };
-  // a thread per pair of horizontally adjacent pixels: each staged row window
-  // serves both pixels' taps (taps in the same row-major order per pixel)
-  static_assert(C5_TW * C5_TH == 2 * C5_T, "two pixels per thread");
-  const int tx2 = threadIdx.x % (C5_TW / 2), py = threadIdx.x / (C5_TW / 2);
-  const int ix0 = X0 + 2 * tx2, iy = Y0 + py;
-  const bool cst = bm == HGB_BOUNDARY_CONSTANT;
-  if (iy < H && ix0 < W) {
-    const bool inner2 = ix0 >= C5_MR && ix0 + 1 < W - C5_MR && iy >= C5_MR && iy < H - C5_MR;
-    if (inner2) {
-      float acc0 = 0.0f, acc1 = 0.0f;
-#pragma unroll
-      for (int oy = 0; oy < C5_MK; ++oy) {
-        // grad_out row iy - (oy - 3), columns ix0 - 3 .. ix0 + 4
-        const float *row = &sd[(py + 2 * C5_MR - oy) * DS_W + 2 * tx2];
-        float v[2 + C5_MK - 1];
-#pragma unroll
-        for (int i = 0; i < 2 + C5_MK - 1; ++i) v[i] = row[i];
-#pragma unroll
-        for (int ox = 0; ox < C5_MK; ++ox) {
-          acc0 = __fmaf_rn(msk[oy * C5_MK + ox], v[2 * C5_MR - ox], acc0);
-          acc1 = __fmaf_rn(msk[oy * C5_MK + ox], v[2 * C5_MR - ox + 1], acc1);
-        }
-      }
-      float *dx = p.dx + (int64_t)b * p.dxb + (int64_t)iy * p.dxp + ix0;
-      dx[0] = acc0;
-      dx[1] = acc1;
-    } else {
-      for (int j = 0; j < 2; ++j) {
-        const int ix = ix0 + j;
-        if (ix >= W) break;
-        float acc = 0.0f;
-        int prx[1 + C5_MR], pry[1 + C5_MR];
-        const int nx = preimages(bm, ix, W, C5_MR, prx), ny = preimages(bm, iy, H, C5_MR, pry);
-        for (int aa = 0; aa < ny; ++aa)
-          for (int c = 0; c < nx; ++c)
-            for (int oy = 0; oy < C5_MK; ++oy)
-              for (int ox = 0; ox < C5_MK; ++ox) {
-                const int jy = pry[aa] - (oy - C5_MR), jx = prx[c] - (ox - C5_MR);
-                if (jx < 0 || jx >= W || jy < 0 || jy >= H) continue;
-                acc = __fmaf_rn(msk[oy * C5_MK + ox], D(jy, jx), acc);
-              }
-        p.dx[(int64_t)b * p.dxb + (int64_t)iy * p.dxp + ix] = acc;
-      }
+    int b, X0, Y0;
+    tile_origin<U_TW, U_TH>(p, tile, b, X0, Y0);
+    const int64_t base = (int64_t)b * p.ib;
+    __syncthreads();  // the previous tile's reads are done
+    for (int cc = threadIdx.x; cc < UD_W * UD_H; cc += C5_T) {
+      const int r = cc / UD_W, k = cc - r * UD_W;
+      const int gy = Y0 - C5_MR + r, gx = X0 - C5_MR + k;
+      sd[cc] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? p.dy1[base + (int64_t)gy * p.ip + gx] : 0.0f;
     }
-    if (p.fuse_dmask) {
-      const float dj0 = D(iy, ix0), dj1 = ix0 + 1 < W ? D(iy, ix0 + 1) : 0.0f;
-      const bool inner_taps = ix0 >= C5_MR && ix0 + 1 < W - C5_MR && iy >= C5_MR && iy < H - C5_MR;
-#pragma unroll
-      for (int oy = 0; oy < C5_MK; ++oy) {
-        // x through the boundary, row iy + oy - 3, columns ix0 - 3 .. ix0 + 4
-        const float *row = &sx[(py + oy) * DS_W + 2 * tx2];
-        float v[2 + C5_MK - 1];
-#pragma unroll
-        for (int i = 0; i < 2 + C5_MK - 1; ++i) v[i] = row[i];
-        const int vy = iy + oy - C5_MR;
-#pragma unroll
-        for (int ox = 0; ox < C5_MK; ++ox) {
-          float t0 = v[ox], t1 = v[ox + 1];
-          if (cst && !inner_taps) {  // CONSTANT taps outside the image carry no gradient
-            const int vx = ix0 + ox - C5_MR;
-            const bool yo = vy < 0 || vy >= H;
-            if (yo || vx < 0 || vx >= W) t0 = 0.0f;
-            if (yo || vx + 1 < 0 || vx + 1 >= W) t1 = 0.0f;
-          }
-          dm[oy * C5_MK + ox] = __fmaf_rn(dj1, t1, __fmaf_rn(dj0, t0, dm[oy * C5_MK + ox]));
-        }
-      }
+    __syncthreads();
+    const int tx = threadIdx.x % U_TW, ty = threadIdx.x / U_TW;
+    for (int py = ty; py < U_TH; py += C5_T / U_TW) {
+      const int ix = X0 + tx, iy = Y0 + py;
+      if (ix >= W || iy >= H) continue;
+      int prx[1 + C5_MR], pry[1 + C5_MR];
+      const int nx = preimages(bm, ix, W, C5_MR, prx), ny = preimages(bm, iy, H, C5_MR, pry);
+      float acc = 0.0f;
+      for (int aa = 0; aa < ny; ++aa)
+        for (int cx = 0; cx < nx; ++cx)
+          for (int oy = 0; oy < C5_MK; ++oy)
+            for (int ox = 0; ox < C5_MK; ++ox) {
+              const int jy = pry[aa] - (oy - C5_MR), jx = prx[cx] - (ox - C5_MR);
+              if (jx < 0 || jx >= W || jy < 0 || jy >= H) continue;
+              acc = __fmaf_rn(msk[oy * C5_MK + ox], sd[(jy - Y0 + C5_MR) * UD_W + jx - X0 + C5_MR], acc);
+            }
+      p.dx[(int64_t)b * p.dxb + (int64_t)iy * p.dxp + ix] = acc;
     }
-  }
-  }  // tiles
-  if (!p.fuse_dmask) return;
-  // block partials of dL/dmask (49 values), FP64 combine by the last block
-#pragma unroll
-  for (int i = 0; i < C5_MK * C5_MK; ++i) {
-    float v = dm[i];
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][i] = v;
-  }
-  __syncthreads();
-  const unsigned int nb = grid_blocks();
-  const unsigned int rank = block_rank() + (unsigned)p.img_offset * nb;
-  if (threadIdx.x < C5_MK * C5_MK) {
-    float s = 0.0f;
-    for (int wv = 0; wv < C5_T / 32; ++wv) s += red[wv][threadIdx.x];
-    p.dm_part[(size_t)rank * C5_MK * C5_MK + threadIdx.x] = s;
-    __threadfence();
-  }
-  if (p.combine && take_last_ticket(p.tickets + 2)) {
-    for (int o = 0; o < C5_MK * C5_MK; ++o) {
-      const double s = block_sum_fixed(
-          (int)nb, [&](int i) { return (double)__ldcg(p.dm_part + (size_t)i * C5_MK * C5_MK + o); }, dsh);
-      if (threadIdx.x == 0) p.grad_mask_dev[o] = (float)s;
-    }
-    if (threadIdx.x == 0) p.tickets[2] = 0u;
   }
 }
 
-// unfused chain: the mask gradient as its own pass over one image
+// the mask gradient as its own pass over one image
 __global__ void __launch_bounds__(C5_T) c5_dmask_kernel(const __grid_constant__ C5Params p) {
   const int b = blockIdx.z + p.img_offset;
   const int o = blockIdx.x;  // one mask tap per block row of the grid
@@ -545,7 +922,7 @@ __global__ void __launch_bounds__(C5_T) c5_dmask_kernel(const __grid_constant__ 
   for (int64_t i = (int64_t)blockIdx.y * C5_T + threadIdx.x; i < (int64_t)p.w * p.h; i += (int64_t)gridDim.y * C5_T) {
     const int jx = (int)(i % p.w), jy = (int)(i / p.w);
     const int ry = remap_c5(p.bmode, jy + oy - C5_MR, p.h), rx = remap_c5(p.bmode, jx + ox - C5_MR, p.w);
-    if (ry == (int)0x80000000 || rx == (int)0x80000000) continue;
+    if (ry == C5_OUT || rx == C5_OUT) continue;
     s = __fmaf_rn(p.dy1[base + (int64_t)jy * p.ip + jx], __ldg(x + (int64_t)ry * p.xp + rx), s);
   }
   __shared__ float sbuf[32];
@@ -553,8 +930,7 @@ __global__ void __launch_bounds__(C5_T) c5_dmask_kernel(const __grid_constant__ 
   if (threadIdx.x == 0) p.dm_part[((size_t)p.img_offset * gridDim.y + blockIdx.y) * C5_MK * C5_MK + o] = v;
 }
 
-// unfused chain: final FP64 combines of the per-image partials (one CTA,
-// fixed order)
+// final FP64 combines of the per-image partials (one CTA, fixed order)
 __global__ void __launch_bounds__(C5_T) c5_combine_kernel(const __grid_constant__ C5Params p, int loss_parts,
                                                           int dc_parts, int dm_parts) {
   __shared__ double dsh[C5_T];
@@ -607,16 +983,17 @@ extern "C" int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, cons
                   "hgb_conv_bilateral_mse: spatial weights must be point-symmetric");
     }
   const int W = x->width, H = x->height, B = x->batch;
-  const int64_t ip = (W + 3) / 4 * 4, ib = ip * H;  // intermediates, floats
-  const dim3 grid(cdiv(W, C5_TW), cdiv(H, C5_TH), B);
-  const size_t nblk = (size_t)grid.x * grid.y * B;
+  const int64_t ip = (W + 3) / 4 * 4, ib = ip * H;  // intermediates, elements
+  const dim3 ugrid(cdiv(W, U_TW), cdiv(H, U_TH), B);
+  const size_t nblk = (size_t)ugrid.x * ugrid.y * B;  // at least the CTAs of any launch below
   const int red_rows = 64;  // row blocks of the unfused mask-gradient pass
   const size_t nparts = std::max(nblk, (size_t)B * red_rows);
-  // workspace: y1, y, a, dy1 images + partials
+  // workspace: the fused form's packed float4 per pixel (or the unfused
+  // form's y1, y, a), then dy1, then the partials
   const size_t img_bytes = (size_t)ib * B * 4;
   const size_t part_bytes = nparts * (8 + 4 + 4 * C5_MK * C5_MK) + 1024;
   Workspace ws;
-  rc = workspace_get(4 * img_bytes + part_bytes, &ws);
+  rc = workspace_get(5 * img_bytes + part_bytes, &ws);
   if (rc) return rc;
   C5Params p;
   memset(&p, 0, sizeof(p));
@@ -627,11 +1004,12 @@ extern "C" int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, cons
   p.xb = x->batch_stride / 4;
   p.tb = t->batch_stride / 4;
   char *wsb = (char *)ws.base;
+  p.pk = (float4 *)wsb;
   p.y1 = (float *)wsb;
   p.y = (float *)(wsb + img_bytes);
   p.a = (float *)(wsb + 2 * img_bytes);
-  p.dy1 = (float *)(wsb + 3 * img_bytes);
-  char *parts = wsb + 4 * img_bytes;
+  p.dy1 = (float *)(wsb + 4 * img_bytes);
+  char *parts = wsb + 5 * img_bytes;
   p.loss_part = (float2 *)parts;
   p.dc_part = (float *)(parts + nparts * 8);
   p.dm_part = (float *)(parts + nparts * 12);
@@ -644,42 +1022,37 @@ extern "C" int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, cons
   p.h = H;
   p.batch = B;
   p.bmode = boundary;
+  p.vec_x = ((uintptr_t)x->data % 16 == 0 && x->pitch % 16 == 0 && x->batch_stride % 16 == 0) ? 1 : 0;
+  p.vec_dx = ((uintptr_t)grad_x->data % 16 == 0 && grad_x->pitch % 16 == 0 && grad_x->batch_stride % 16 == 0) ? 1 : 0;
   p.mask_dev = mask_dev;
   p.sigma_dev = sigma_dev;
-  for (int i = 0; i < C5_BK * C5_BK; ++i) {
-    p.sm[i] = smask[i];
+  for (int i = 0; i < C5_BK * C5_BK; ++i)
     p.lsm[i] = smask[i] > 0.0f ? (float)std::log2((double)smask[i]) : -INFINITY;
-  }
   p.inv_n = 1.0 / ((double)B * W * H);
   p.tickets = ws.tickets + 8;
   p.loss_dev = loss_dev;
   p.grad_mask_dev = grad_mask_dev;
   p.grad_sigma_dev = grad_sigma_dev;
-  p.tiles_x = (int)grid.x;
-  p.tiles_y = (int)grid.y;
   cudaStream_t st = (cudaStream_t)stream;
-  // persistent grids: one wave of resident CTAs walking the tiles
-  const int occ[3] = {resident_ctas((const void *)c5_forward_kernel, C5_T, 0),
-                      resident_ctas((const void *)c5_bilateral_adjoint_kernel, C5_T, 0),
-                      resident_ctas((const void *)c5_conv_adjoint_kernel, C5_T, 0)};
-  auto wave = [&](int k, int ntiles) { return std::max(1, std::min(ntiles, num_sms() * occ[k])); };
   cudaEvent_t ev = before_launch(st);
   if (mode == 0) {
-    p.fuse_conv = 1;
-    p.fuse_loss = 1;
-    p.symmetric = 1;
-    p.fuse_dmask = 1;
-    p.combine = 1;
-    p.ntiles = (int)nblk;
-    c5_forward_kernel<<<wave(0, p.ntiles), C5_T, 0, st>>>(p);
-    c5_bilateral_adjoint_kernel<<<wave(1, p.ntiles), C5_T, 0, st>>>(p);
-    c5_conv_adjoint_kernel<<<wave(2, p.ntiles), C5_T, 0, st>>>(p);
+    // persistent grids: one wave of resident CTAs walking the tiles
+    p.tiles_x = cdiv(W, F_TW);
+    p.tiles_y = cdiv(H, F_TH);
+    p.ntiles = p.tiles_x * p.tiles_y * B;
+    auto wave = [&](const void *k) { return std::max(1, std::min(p.ntiles, num_sms() * resident_ctas(k, C5_T, 0))); };
+    c5_forward_kernel<<<wave((const void *)c5_forward_kernel), C5_T, 0, st>>>(p);
+    c5_bilateral_adjoint_kernel<<<wave((const void *)c5_bilateral_adjoint_kernel), C5_T, 0, st>>>(p);
+    c5_conv_adjoint_kernel<<<wave((const void *)c5_conv_adjoint_kernel), C5_T, 0, st>>>(p);
     return after_launch("c5 fused", st, ev);
   }
   // unfused chain, one image at a time
-  const dim3 g1(grid.x, grid.y, 1);
-  const int per_image = (int)(grid.x * grid.y);
-  const int g_bil = wave(1, per_image);
+  p.tiles_x = (int)ugrid.x;
+  p.tiles_y = (int)ugrid.y;
+  const dim3 g1(ugrid.x, ugrid.y, 1);
+  const int per_image = (int)(ugrid.x * ugrid.y);
+  auto wave = [&](const void *k) { return std::max(1, std::min(per_image, num_sms() * resident_ctas(k, C5_T, 0))); };
+  const int g_bil = wave((const void *)c5u_bilateral_adjoint_kernel);
   for (int b = 0; b < B; ++b) {
     hgb_view xv{(void *)(p.x + (int64_t)b * p.xb), HGB_F32, W, H, 1, x->pitch, x->pitch * H};
     hgb_view yv{p.y1 + (int64_t)b * ib, HGB_F32, W, H, 1, ip * 4, ib * 4};
@@ -688,16 +1061,11 @@ extern "C" int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, cons
     if (rc) return rc;
     C5Params q = p;
     q.img_offset = b;
-    q.fuse_conv = 0;
-    q.fuse_loss = 0;
-    q.symmetric = 0;
-    q.fuse_dmask = 0;
-    q.combine = 0;
     q.ntiles = per_image;
-    c5_forward_kernel<<<wave(0, per_image), C5_T, 0, st>>>(q);
+    c5u_forward_kernel<<<wave((const void *)c5u_forward_kernel), C5_T, 0, st>>>(q);
     c5_alpha_kernel<<<g1, C5_T, 0, st>>>(q);
-    c5_bilateral_adjoint_kernel<<<g_bil, C5_T, 0, st>>>(q);
-    c5_conv_adjoint_kernel<<<wave(2, per_image), C5_T, 0, st>>>(q);
+    c5u_bilateral_adjoint_kernel<<<g_bil, C5_T, 0, st>>>(q);
+    c5u_conv_adjoint_kernel<<<wave((const void *)c5u_conv_adjoint_kernel), C5_T, 0, st>>>(q);
     c5_dmask_kernel<<<dim3(C5_MK * C5_MK, red_rows, 1), C5_T, 0, st>>>(q);
   }
   c5_combine_kernel<<<1, C5_T, 0, st>>>(p, (int)nblk, B * g_bil, B * red_rows);

@@ -64,6 +64,27 @@ def test_adjoint_vs_fp64_oracle(gpu, oracle, boundary, mode):
     assert abs(ds - ds0) <= ADJ_TOL * abs(ds0), (ds, ds0)
 
 
+@pytest.mark.parametrize("hw", [(8, 8), (9, 13), (21, 67), (70, 131), (37, 2 * 64 + 6)])
+@pytest.mark.parametrize("boundary", [1, 3, 4])
+def test_adjoint_ragged_shapes(gpu, oracle, hw, boundary):
+    """Images from the 8 x 8 minimum up to several tiles with ragged edges: the
+    fused form splits the pixels into tiles and the edge bands (radius 4 for
+    the bilateral, 3 for the convolution), the unfused form does not; both
+    against the FP64 oracle."""
+    H, W = hw
+    x, t, mask, sm = _setup(oracle, 2, H, W, boundary, 70 + H + W + boundary)
+    L0, dx0, dm0, ds0 = _oracle_batch(oracle, x, t, mask, sm, 0.15, boundary)
+    for mode in (0, 1):
+        L, dx, dm, ds = _gpu(gpu, x, t, mask, 0.15, sm, boundary, mode)
+        assert abs(L - L0) <= LOSS_TOL * abs(L0), (mode, L, L0)
+        assert rel(dx, dx0) <= ADJ_TOL, (mode, rel(dx, dx0))
+        assert rel(dm, dm0) <= ADJ_TOL, (mode, rel(dm, dm0))
+        assert abs(ds - ds0) <= ADJ_TOL * abs(ds0), (mode, ds, ds0)
+        # no pixel off: the band pixels are a small share of the larger images
+        err = np.abs(dx - dx0)
+        assert np.max(err) <= 1e-4 * np.max(np.abs(dx0)), (mode, np.unravel_index(np.argmax(err), err.shape))
+
+
 @pytest.mark.parametrize("boundary", [1, 3])
 def test_adjoint_vs_central_differences(gpu, oracle, boundary):
     """FP64 central differences (eps = 1e-4) of the FP64 forward on a 64x64 crop."""
