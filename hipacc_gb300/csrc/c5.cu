@@ -58,6 +58,7 @@
 #include <cstring>
 
 #include "reduce_common.cuh"
+#include "tma.cuh"
 
 namespace hgb {
 namespace {
@@ -76,7 +77,9 @@ constexpr int F_TW = 64, F_TH = 16, F_GX = F_TW / 4;
 constexpr int FX_R = C5_MR + C5_BR;                          // radius of the staged x
 constexpr int FX_W = F_TW + 16, FX_H = F_TH + 2 * FX_R;      // x: columns X0-8 .. X0+71, rows Y0-7 ..
 constexpr int FY_W = F_TW + 2 * C5_BR, FY_H = F_TH + 2 * C5_BR;  // u / staged pairs: columns X0-4 .., rows Y0-4 ..
-constexpr int FC_W = F_TW + 8, FC_H = F_TH + 2 * C5_MR;      // dy1 / x pairs: columns X0-4 .., rows Y0-3 ..
+constexpr int FC_W = F_TW + 8, FC_H = F_TH + 2 * C5_MR;      // dy1 / x: columns X0-4 .., rows Y0-3 ..
+constexpr int FX_N = FX_W * FX_H, FC_N = 1600;                // floats per staged array (128-byte multiples)
+static_assert(FX_N % 32 == 0 && FC_W * FC_H <= FC_N && FC_N % 32 == 0, "TMA destinations stay 128-byte aligned");
 static_assert(F_GX * F_TH == C5_T, "16 x 16 threads");
 // Staged rows of pairs are skewed by one element every 8 (16-byte elements)
 // or every 16 (8-byte elements): a thread reads positions 4 tx + s, and
@@ -84,13 +87,17 @@ static_assert(F_GX * F_TH == C5_T, "16 x 16 threads");
 // 2 (4) bank groups.
 constexpr int SQ_W = FY_W + FY_W / 8;   // float4 pairs (u, a)
 constexpr int SB_W = FY_W + FY_W / 16;  // float2 pairs (B)
-constexpr int SC_W = FC_W + FC_W / 16;  // float2 pairs (dy1, x)
 __host__ __device__ constexpr int skew8(int k) { return k + (k >> 3); }
 __host__ __device__ constexpr int skew16(int k) { return k + (k >> 4); }
-static_assert(skew8(FY_W - 1) < SQ_W && skew16(FY_W - 1) < SB_W && skew16(FC_W - 1) < SC_W, "skewed rows");
+static_assert(skew8(FY_W - 1) < SQ_W && skew16(FY_W - 1) < SB_W, "skewed rows");
 static_assert(FY_H * (FY_W / 8) <= C5_T, "one group of eight y1 cells per thread");
 
 struct C5Params {
+  CUtensorMap map_xf;      // x, box FX_W x FX_H (forward)
+  CUtensorMap map_xc;      // x, box FC_W x FC_H (conv adjoint)
+  CUtensorMap map_g;       // dy1, box FC_W x FC_H (conv adjoint)
+  int use_tma;             // the maps are valid (x TMA-legal); else plain loads
+  int *status;             // device status word (bounded waits)
   const float *x, *t;
   int64_t xp, tp, xb, tb;  // pitches / batch strides in floats
   float4 *pk;              // fused: per pixel (u, a, -a u_y, u_y)
@@ -264,13 +271,41 @@ __device__ __forceinline__ void bil_tap(f2 V, f2 C, f2 NL, f2 &Ws, f2 &Ns) {
   Ns = f2_fma(e, V, Ns);
 }
 
+// One thread issues the TMA loads of a tile's staged boxes on the stage's
+// barrier.
+__device__ __forceinline__ void c5_issue(uint64_t *bar, unsigned bytes, void *d0, const CUtensorMap *m0, void *d1,
+                                         const CUtensorMap *m1, int x, int y, int b) {
+  mbar_expect_tx(bar, bytes);
+  tma_load_3d(d0, m0, x, y, b, bar);
+  if (d1) tma_load_3d(d1, m1, x, y, b, bar);
+}
+
+// Bounded wait for stage s of tile iteration i; on expiry records the status
+// and waits (bounded) for the loads still in flight, the next tile's included.
+__device__ __forceinline__ bool c5_wait(const C5Params &p, uint64_t *bars, int i, bool next_issued) {
+  const int s = i & 1;
+  if (cta_wait(&bars[s], (i >> 1) & 1)) return true;
+  if (threadIdx.x == 0) {
+    record_status(p.status, HGB_ERR_TIMEOUT);
+    mbar_wait(&bars[s], (i >> 1) & 1);
+    if (next_issued) mbar_wait(&bars[s ^ 1], ((i + 1) >> 1) & 1);
+  }
+  return false;
+}
+
 __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant__ C5Params p) {
-  __shared__ __align__(16) float xs[FX_H * FX_W];
+  __shared__ __align__(128) float xst[2][FX_N];  // x: double-buffered TMA stages
   __shared__ __align__(16) float us[FY_H * FY_W];
   __shared__ f2 m2[C5_MK * C5_MK];
   __shared__ f2 nl2[C5_BK * C5_BK];
-  __shared__ double dsh[C5_T];
+  __shared__ __align__(8) uint64_t bars[2];
+  double *dsh = reinterpret_cast<double *>(&xst[0][0]);  // the final combine, after the tiles
   const int W = p.w, H = p.h, bm = p.bmode;
+  if (p.use_tma && threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_fence_init();
+  }
   for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) {
     const float m = __ldg(p.mask_dev + i);
     m2[i] = f2_pack(m, m);
@@ -282,26 +317,57 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
   const float g_scale = (float)(2.0 * p.inv_n);
   const int tx = threadIdx.x % F_GX, ty = threadIdx.x / F_GX;
   Kahan lsum{0.0f, 0.0f};
-  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+  __syncthreads();  // barriers initialised
+  auto issue = [&](int tile, int s) {
+    int b, X0, Y0;
+    tile_origin<F_TW, F_TH>(p, tile, b, X0, Y0);
+    c5_issue(&bars[s], FX_N * 4, xst[s], &p.map_xf, nullptr, nullptr, X0 - 8, Y0 - FX_R, b);
+  };
+  if (p.use_tma && threadIdx.x == 0) issue(blockIdx.x, 0);
+  int it = 0;
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++it) {
     int b, X0, Y0;
     tile_origin<F_TW, F_TH>(p, tile, b, X0, Y0);
     const float *x = p.x + (int64_t)b * p.xb;
-    __syncthreads();  // the previous tile's reads of xs / us are done
+    const bool edge = !(X0 >= 8 && X0 + F_TW + 8 <= W && Y0 >= FX_R && Y0 + F_TH + FX_R <= H);
+    float *xs = xst[p.use_tma ? (it & 1) : 0];
     // x on rows Y0-7 .., columns X0-8 .. through the boundary
-    if (p.vec_x && X0 >= 8 && X0 + F_TW + 8 <= W && Y0 >= FX_R && Y0 + F_TH + FX_R <= H) {
-      for (int c4 = threadIdx.x; c4 < FX_H * (FX_W / 4); c4 += C5_T) {
-        const int r = c4 / (FX_W / 4), k4 = c4 - r * (FX_W / 4);
-        reinterpret_cast<float4 *>(xs)[c4] =
-            __ldg(reinterpret_cast<const float4 *>(x + (int64_t)(Y0 - FX_R + r) * p.xp + X0 - 8) + k4);
+    if (p.use_tma) {
+      // the next tile's box lands while this one computes (its stage was last
+      // read by the convolution of the previous tile, before a CTA barrier)
+      const bool next = tile + (int)gridDim.x < p.ntiles;
+      if (next && threadIdx.x == 0) {
+        fence_proxy_async_smem();
+        issue(tile + gridDim.x, (it & 1) ^ 1);
+      }
+      if (!c5_wait(p, bars, it, next)) break;
+      if (edge) {  // cells outside the image (zero-filled) through the boundary
+        for (int cc = threadIdx.x; cc < FX_N; cc += C5_T) {
+          const int r = cc / FX_W, k = cc - r * FX_W;
+          const int vy = Y0 - FX_R + r, vx = X0 - 8 + k;
+          if (vy >= 0 && vy < H && vx >= 0 && vx < W) continue;
+          const int ry = remap_c5(bm, vy, H), rx = remap_c5(bm, vx, W);
+          xs[cc] = (ry == C5_OUT || rx == C5_OUT) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
+        }
+        __syncthreads();
       }
     } else {
-      for (int cc = threadIdx.x; cc < FX_H * FX_W; cc += C5_T) {
-        const int r = cc / FX_W, k = cc - r * FX_W;
-        const int ry = remap_c5(bm, Y0 - FX_R + r, H), rx = remap_c5(bm, X0 - 8 + k, W);
-        xs[cc] = (ry == C5_OUT || rx == C5_OUT) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
+      __syncthreads();  // the previous tile's reads of xs are done
+      if (p.vec_x && !edge) {
+        for (int c4 = threadIdx.x; c4 < FX_H * (FX_W / 4); c4 += C5_T) {
+          const int r = c4 / (FX_W / 4), k4 = c4 - r * (FX_W / 4);
+          reinterpret_cast<float4 *>(xs)[c4] =
+              __ldg(reinterpret_cast<const float4 *>(x + (int64_t)(Y0 - FX_R + r) * p.xp + X0 - 8) + k4);
+        }
+      } else {
+        for (int cc = threadIdx.x; cc < FX_N; cc += C5_T) {
+          const int r = cc / FX_W, k = cc - r * FX_W;
+          const int ry = remap_c5(bm, Y0 - FX_R + r, H), rx = remap_c5(bm, X0 - 8 + k, W);
+          xs[cc] = (ry == C5_OUT || rx == C5_OUT) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
     // u = q y1 on rows Y0-4 .., columns X0-4 ..: eight cells per thread from
     // one 16-value row window of x per mask row, taps row-major (y1 exactly as
     // hgb_local_op computes it)
@@ -557,52 +623,79 @@ __global__ void __launch_bounds__(C5_T, 4) c5_bilateral_adjoint_kernel(const __g
   }
 }
 
-// stage one row segment of four positions k .. k+3 (k a multiple of 4, so the
-// skewed positions are consecutive) as pairs (v_k, v_k+1): in-image values,
-// zero elsewhere
-__device__ __forceinline__ void stage_pairs4(f2 *dst, const float *row, int gx, int W, bool vec) {
-  float v[5];
-  if (vec && gx >= 0 && gx + 4 < W) {
-    const float4 a = __ldg(reinterpret_cast<const float4 *>(row + gx));
-    v[0] = a.x;
-    v[1] = a.y;
-    v[2] = a.z;
-    v[3] = a.w;
-    v[4] = __ldg(row + gx + 4);
-  } else {
-#pragma unroll
-    for (int i = 0; i < 5; ++i) v[i] = (gx + i >= 0 && gx + i < W) ? __ldg(row + gx + i) : 0.0f;
+// stage rows Y0-3 .., columns X0-4 .. of one image plane without TMA (zero
+// outside the image)
+__device__ __forceinline__ void c5_stage_plain(float *dst, const float *src, int64_t pitch, int X0, int Y0, int W,
+                                               int H, bool vec) {
+  for (int it = threadIdx.x; it < FC_H * (FC_W / 4); it += C5_T) {
+    const int r = it / (FC_W / 4), k = (it - r * (FC_W / 4)) * 4;
+    const int gy = Y0 - C5_MR + r, gx = X0 - 4 + k;
+    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (gy >= 0 && gy < H) {
+      const float *row = src + (int64_t)gy * pitch;
+      if (vec && gx >= 0 && gx + 3 < W) {
+        v = __ldg(reinterpret_cast<const float4 *>(row + gx));
+      } else {
+        v.x = (gx >= 0 && gx < W) ? __ldg(row + gx) : 0.0f;
+        v.y = (gx + 1 >= 0 && gx + 1 < W) ? __ldg(row + gx + 1) : 0.0f;
+        v.z = (gx + 2 >= 0 && gx + 2 < W) ? __ldg(row + gx + 2) : 0.0f;
+        v.w = (gx + 3 >= 0 && gx + 3 < W) ? __ldg(row + gx + 3) : 0.0f;
+      }
+    }
+    *reinterpret_cast<float4 *>(&dst[r * FC_W + k]) = v;
   }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) dst[i] = f2_pack(v[i], v[i + 1]);
 }
 
-__global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_constant__ C5Params p) {
-  __shared__ __align__(16) f2 sg[FC_H * SC_W];  // (dy1_k, dy1_k+1)
-  __shared__ __align__(16) f2 sx[FC_H * SC_W];  // (x_k, x_k+1)
-  __shared__ f2 m2[C5_MK * C5_MK];
+// a row window of twelve staged values (three aligned 16-byte loads)
+__device__ __forceinline__ void c5_window12(const float *row, float (&w)[12]) {
+#pragma unroll
+  for (int v = 0; v < 3; ++v) {
+    const float4 t4 = reinterpret_cast<const float4 *>(row)[v];
+    w[4 * v] = t4.x;
+    w[4 * v + 1] = t4.y;
+    w[4 * v + 2] = t4.z;
+    w[4 * v + 3] = t4.w;
+  }
+}
+
+__global__ void __launch_bounds__(C5_T, 2) c5_conv_adjoint_kernel(const __grid_constant__ C5Params p) {
+  __shared__ __align__(128) float stg[2][2][FC_N];  // [stage][dy1, x]: TMA double buffer
+  __shared__ __align__(16) f2 m2[C5_MK][8];        // mask pairs (m, m); the eighth is padding
   __shared__ float msk[C5_MK * C5_MK];
   __shared__ float red[C5_T / 32][C5_MK * C5_MK];
-  __shared__ double dsh[C5_T];
+  __shared__ __align__(8) uint64_t bars[2];
+  double *dsh = reinterpret_cast<double *>(&stg[0][0][0]);  // the final combine, after the tiles
   const int W = p.w, H = p.h, bm = p.bmode;
-  for (int i = threadIdx.x; i < C5_MK * C5_MK; i += C5_T) {
-    const float m = __ldg(p.mask_dev + i);
-    msk[i] = m;
-    m2[i] = f2_pack(m, m);
+  for (int i = threadIdx.x; i < C5_MK * 8; i += C5_T) {
+    const int oy = i / 8, ox = i - oy * 8;
+    const float m = ox < C5_MK ? __ldg(p.mask_dev + oy * C5_MK + ox) : 0.0f;
+    m2[oy][ox] = f2_pack(m, m);
+    if (ox < C5_MK) msk[oy * C5_MK + ox] = m;
   }
+  if (p.use_tma && threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  auto issue = [&](int tile, int s) {
+    int b, X0, Y0;
+    tile_origin<F_TW, F_TH>(p, tile, b, X0, Y0);
+    c5_issue(&bars[s], 2 * FC_W * FC_H * 4, stg[s][0], &p.map_g, stg[s][1], &p.map_xc, X0 - 4, Y0 - C5_MR, b);
+  };
+  // the first tile's boxes land while the band's grad_in runs
+  if (p.use_tma && threadIdx.x == 0) issue(blockIdx.x, 0);
   // band pixels of every image of the batch, an equal contiguous share per
   // CTA; first part (before the mask-gradient registers are live): grad_in
   // through the pre-images
   const int band_per = band_size(W, H, C5_MR);
   int64_t k0, k1;
   cta_share((int64_t)band_per * p.batch, k0, k1);
-  __syncthreads();  // msk
   for (int64_t k = k0 + threadIdx.x; k < k1; k += C5_T) {
     const int b = (int)(k / band_per);
     int jy, jx;
     band_pos((int)(k - (int64_t)b * band_per), W, H, C5_MR, jy, jx);
     const float *g = p.dy1 + (int64_t)b * p.ib;
-    // grad_in through the pre-images of j
     int prx[1 + C5_MR], pry[1 + C5_MR];
     const int nx = preimages(bm, jx, W, C5_MR, prx), ny = preimages(bm, jy, H, C5_MR, pry);
     float acc = 0.0f;
@@ -627,40 +720,46 @@ __global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_cons
   for (int i = 0; i < C5_MK; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) DM[i][j] = 0ull;
-  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+  int it = 0;
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++it) {
     int b, X0, Y0;
     tile_origin<F_TW, F_TH>(p, tile, b, X0, Y0);
-    const float *g = p.dy1 + (int64_t)b * p.ib;
-    const float *x = p.x + (int64_t)b * p.xb;
-    __syncthreads();  // the previous tile's reads are done
-    // rows Y0-3 .., columns X0-4 ..: four positions per item
-    for (int it = threadIdx.x; it < FC_H * (FC_W / 4); it += C5_T) {
-      const int r = it / (FC_W / 4), k = (it - r * (FC_W / 4)) * 4;
-      const int gy = Y0 - C5_MR + r, gx = X0 - 4 + k;
-      if (gy < 0 || gy >= H) continue;
-      stage_pairs4(&sg[r * SC_W + skew16(k)], g + (int64_t)gy * p.ip, gx, W, true);
-      stage_pairs4(&sx[r * SC_W + skew16(k)], x + (int64_t)gy * p.xp, gx, W, p.vec_x);
+    const int s = p.use_tma ? (it & 1) : 0;
+    if (p.use_tma) {
+      // the next tile's boxes land while this one computes
+      const bool next = tile + (int)gridDim.x < p.ntiles;
+      if (next && threadIdx.x == 0) {
+        fence_proxy_async_smem();
+        issue(tile + gridDim.x, s ^ 1);
+      }
+      if (!c5_wait(p, bars, it, next)) break;
+    } else {
+      c5_stage_plain(stg[0][0], p.dy1 + (int64_t)b * p.ib, p.ip, X0, Y0, W, H, true);
+      c5_stage_plain(stg[0][1], p.x + (int64_t)b * p.xb, p.xp, X0, Y0, W, H, p.vec_x);
+      __syncthreads();
     }
-    __syncthreads();
+    const float *sg = stg[s][0], *sx = stg[s][1];
     const int jx0 = X0 + 4 * tx, jy = Y0 + ty;
     if (jx0 >= 4 && jx0 + 3 < W - C5_MR && jy >= C5_MR && jy < H - C5_MR) {
-      // skewed position 4 tx + s of a row = base + s + (s < 4 ? 0 : s < 8 ? k1 : k2)
-      const int b1 = (tx & 3) == 3, b2 = (tx & 3) >= 2, base = 4 * tx + (tx >> 2);
-      auto at = [&](const f2 *row, int s) { return row[s + (s < 4 ? 0 : s < 8 ? b1 : b2)]; };
-      // grad_in: pixel pair pp at position 4 tx + 4 + 2 pp gathers dy1 at
-      // positions 4 tx + 7 + 2 pp - ox of row ty + 6 - oy
+      // grad_in: pixel pair pp (columns 4 tx + 4 + 2 pp ..) gathers dy1 at
+      // columns 4 tx + 7 + 2 pp - ox of row ty + 6 - oy
       f2 GI0 = 0ull, GI1 = 0ull;
 #pragma unroll
       for (int oy = 0; oy < C5_MK; ++oy) {
-        const f2 *row = &sg[(ty + 2 * C5_MR - oy) * SC_W + base];
-        f2 gw[9];
+        float w[12];
+        c5_window12(&sg[(ty + 2 * C5_MR - oy) * FC_W + 4 * tx], w);
+        const float4 *mr = reinterpret_cast<const float4 *>(&m2[oy][0]);
 #pragma unroll
-        for (int s = 0; s < 9; ++s) gw[s] = at(row, s + 1);
+        for (int o2 = 0; o2 < 4; ++o2) {
+          const float4 mm = mr[o2];  // taps 2 o2, 2 o2 + 1 as pairs (m, m)
 #pragma unroll
-        for (int ox = 0; ox < C5_MK; ++ox) {
-          const f2 M = m2[oy * C5_MK + ox];
-          GI0 = f2_fma(M, gw[6 - ox], GI0);
-          GI1 = f2_fma(M, gw[8 - ox], GI1);
+          for (int l = 0; l < 2; ++l) {
+            const int ox = 2 * o2 + l;
+            if (ox >= C5_MK) continue;
+            const f2 M = l ? f2_pack(mm.z, mm.w) : f2_pack(mm.x, mm.y);
+            GI0 = f2_fma(M, f2_pack(w[7 - ox], w[8 - ox]), GI0);
+            GI1 = f2_fma(M, f2_pack(w[9 - ox], w[10 - ox]), GI1);
+          }
         }
       }
       float *dxr = p.dx + (int64_t)b * p.dxb + (int64_t)jy * p.dxp + jx0;
@@ -672,23 +771,22 @@ __global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_cons
         dxr[2] = f2_lo(GI1);
         dxr[3] = f2_hi(GI1);
       }
-      // mask gradient: pixel i (position 4 tx + 4 + i) with x at positions
+      // mask gradient: pixel i (column 4 tx + 4 + i) with x at columns
       // 4 tx + 1 + i + ox of row ty + oy
-      const f2 gc0 = at(&sg[(ty + C5_MR) * SC_W + base], 4), gc1 = at(&sg[(ty + C5_MR) * SC_W + base], 6);
-      const f2 GG[4] = {f2_pack(f2_lo(gc0), f2_lo(gc0)), f2_pack(f2_hi(gc0), f2_hi(gc0)),
-                        f2_pack(f2_lo(gc1), f2_lo(gc1)), f2_pack(f2_hi(gc1), f2_hi(gc1))};
+      const float4 gc = *reinterpret_cast<const float4 *>(&sg[(ty + C5_MR) * FC_W + 4 * tx + 4]);
+      const f2 GG[4] = {f2_pack(gc.x, gc.x), f2_pack(gc.y, gc.y), f2_pack(gc.z, gc.z), f2_pack(gc.w, gc.w)};
 #pragma unroll
       for (int oy = 0; oy < C5_MK; ++oy) {
-        const f2 *row = &sx[(ty + oy) * SC_W + base];
-        f2 xw[12];
-#pragma unroll
-        for (int s = 0; s < 12; ++s) xw[s] = at(row, s);
+        float xw[12];
+        c5_window12(&sx[(ty + oy) * FC_W + 4 * tx], xw);
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int op = 0; op < 4; ++op) DM[oy][op] = f2_fma(GG[i], xw[1 + i + 2 * op], DM[oy][op]);
+          for (int op = 0; op < 4; ++op)
+            DM[oy][op] = f2_fma(GG[i], f2_pack(xw[1 + i + 2 * op], xw[2 + i + 2 * op]), DM[oy][op]);
       }
     }
+    __syncthreads();  // every thread is done with this stage before it is reloaded
   }  // tiles
   // band pixels, second part: their mask-gradient terms
   for (int64_t k = k0 + threadIdx.x; k < k1; k += C5_T) {
@@ -697,7 +795,7 @@ __global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_cons
     band_pos((int)(k - (int64_t)b * band_per), W, H, C5_MR, jy, jx);
     const float *g = p.dy1 + (int64_t)b * p.ib;
     const float *x = p.x + (int64_t)b * p.xb;
-    // mask gradient with x through the boundary (CONSTANT taps outside carry none)
+    // x through the boundary (CONSTANT taps outside carry none)
     const float gj = g[(int64_t)jy * p.ip + jx];
     const f2 GJ = f2_pack(gj, gj);
     int rx[2 * 4];
@@ -729,16 +827,16 @@ __global__ void __launch_bounds__(C5_T) c5_conv_adjoint_kernel(const __grid_cons
   __syncthreads();
   const unsigned int nb = grid_blocks();
   if (threadIdx.x < C5_MK * C5_MK) {
-    float s = 0.0f;
-    for (int wv = 0; wv < C5_T / 32; ++wv) s += red[wv][threadIdx.x];
-    p.dm_part[(size_t)block_rank() * C5_MK * C5_MK + threadIdx.x] = s;
+    float sum = 0.0f;
+    for (int wv = 0; wv < C5_T / 32; ++wv) sum += red[wv][threadIdx.x];
+    p.dm_part[(size_t)block_rank() * C5_MK * C5_MK + threadIdx.x] = sum;
     __threadfence();
   }
   if (take_last_ticket(p.tickets + 2)) {
     for (int o = 0; o < C5_MK * C5_MK; ++o) {
-      const double s = block_sum_fixed(
+      const double sum = block_sum_fixed(
           (int)nb, [&](int i) { return (double)__ldcg(p.dm_part + (size_t)i * C5_MK * C5_MK + o); }, dsh);
-      if (threadIdx.x == 0) p.grad_mask_dev[o] = (float)s;
+      if (threadIdx.x == 0) p.grad_mask_dev[o] = (float)sum;
     }
     if (threadIdx.x == 0) p.tickets[2] = 0u;
   }
@@ -1033,6 +1131,16 @@ extern "C" int hgb_conv_bilateral_mse(const hgb_view *x, const hgb_view *t, cons
   p.loss_dev = loss_dev;
   p.grad_mask_dev = grad_mask_dev;
   p.grad_sigma_dev = grad_sigma_dev;
+  if (mode == 0 && tma_legal(x->data, x->pitch, x->batch_stride, B) &&
+      make_tensor_map_3d(&p.map_xf, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, x->data, W, H, B, x->pitch, x->batch_stride,
+                         FX_W, FX_H) == HGB_OK &&
+      make_tensor_map_3d(&p.map_xc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, x->data, W, H, B, x->pitch, x->batch_stride,
+                         FC_W, FC_H) == HGB_OK &&
+      make_tensor_map_3d(&p.map_g, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p.dy1, W, H, B, ip * 4, ib * 4, FC_W, FC_H) ==
+          HGB_OK) {
+    p.use_tma = 1;
+    p.status = device_status_word();
+  }
   cudaStream_t st = (cudaStream_t)stream;
   cudaEvent_t ev = before_launch(st);
   if (mode == 0) {

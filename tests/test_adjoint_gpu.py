@@ -85,6 +85,23 @@ def test_adjoint_ragged_shapes(gpu, oracle, hw, boundary):
         assert np.max(err) <= 1e-4 * np.max(np.abs(dx0)), (mode, np.unravel_index(np.argmax(err), err.shape))
 
 
+@pytest.mark.parametrize("boundary", [1, 3, 4])
+def test_adjoint_padded_rows_equal_dense(gpu, oracle, boundary):
+    """Rows padded to a pitch that is not a multiple of 16 bytes rule out the
+    TMA staging: the plain-load staging must give bit-identical results."""
+    x, t, mask, sm = _setup(oracle, 2, 70, 150, boundary, 90 + boundary)
+    xd = torch.from_numpy(x).cuda()
+    xp = torch.zeros((2, 70, 151), dtype=torch.float32, device="cuda")
+    xp[:, :, :150] = xd
+    args = (torch.from_numpy(t).cuda(), torch.from_numpy(mask).cuda(),
+            torch.tensor([0.15], dtype=torch.float32, device="cuda"), sm, boundary, 0)
+    a = gpu.conv_bilateral_mse(xd, *args)
+    b = gpu.conv_bilateral_mse(xp[:, :, :150], *args)
+    torch.cuda.synchronize()
+    for u, v in zip(a, b):
+        assert torch.equal(u, v)
+
+
 @pytest.mark.parametrize("boundary", [1, 3])
 def test_adjoint_vs_central_differences(gpu, oracle, boundary):
     """FP64 central differences (eps = 1e-4) of the FP64 forward on a 64x64 crop."""
