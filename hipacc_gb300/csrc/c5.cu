@@ -75,11 +75,16 @@ constexpr int UD_W = U_TW + 2 * C5_MR, UD_H = U_TH + 2 * C5_MR;  // dy1 / x (rad
 // fused kernels: 64 x 16 tiles, four pixels per thread
 constexpr int F_TW = 64, F_TH = 16, F_GX = F_TW / 4;
 constexpr int FX_R = C5_MR + C5_BR;                          // radius of the staged x
-constexpr int FX_W = F_TW + 16, FX_H = F_TH + 2 * FX_R;      // x: columns X0-8 .. X0+71, rows Y0-7 ..
+// x: columns X0-8 .. X0+75 (the convolution reads up to X0+70; a row of 84
+// floats puts eight consecutive rows on distinct 16-byte bank groups), rows Y0-7 ..
+constexpr int FX_W = F_TW + 20, FX_H = F_TH + 2 * FX_R;
 constexpr int FY_W = F_TW + 2 * C5_BR, FY_H = F_TH + 2 * C5_BR;  // u / staged pairs: columns X0-4 .., rows Y0-4 ..
 constexpr int FC_W = F_TW + 8, FC_H = F_TH + 2 * C5_MR;      // dy1 / x: columns X0-4 .., rows Y0-3 ..
-constexpr int FX_N = FX_W * FX_H, FC_N = 1600;                // floats per staged array (128-byte multiples)
-static_assert(FX_N % 32 == 0 && FC_W * FC_H <= FC_N && FC_N % 32 == 0, "TMA destinations stay 128-byte aligned");
+constexpr int NL_W = C5_BK + 1;  // range-weight pairs per mask row, padded for 16-byte loads
+constexpr int US_W = FY_W + 4;  // row stride of the forward's u (eight consecutive rows on distinct bank groups)
+constexpr int FX_N = 2528, FC_N = 1600;  // floats per staged array (128-byte multiples)
+static_assert(FX_W * FX_H <= FX_N && FX_N % 32 == 0 && FC_W * FC_H <= FC_N && FC_N % 32 == 0,
+              "TMA destinations stay 128-byte aligned");
 static_assert(F_GX * F_TH == C5_T, "16 x 16 threads");
 // Staged rows of pairs are skewed by one element every 8 (16-byte elements)
 // or every 16 (8-byte elements): a thread reads positions 4 tx + s, and
@@ -262,6 +267,16 @@ __device__ __forceinline__ void loss_publish(const C5Params &p, Kahan lsum, doub
 
 // ================================================================== fused form
 
+// a mask row of range-weight pairs, two per 16-byte load
+__device__ __forceinline__ void nl_row(const f2 *row, f2 (&o)[NL_W]) {
+#pragma unroll
+  for (int i = 0; i < NL_W / 2; ++i) {
+    const ulonglong2 v = reinterpret_cast<const ulonglong2 *>(row)[i];
+    o[2 * i] = v.x;
+    o[2 * i + 1] = v.y;
+  }
+}
+
 // one bilateral tap for a pixel pair: weight e = exp2(-(d'^2 + nl))
 __device__ __forceinline__ void bil_tap(f2 V, f2 C, f2 NL, f2 &Ws, f2 &Ns) {
   const f2 d = f2_sub(V, C);
@@ -293,11 +308,11 @@ __device__ __forceinline__ bool c5_wait(const C5Params &p, uint64_t *bars, int i
   return false;
 }
 
-__global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant__ C5Params p) {
+__global__ void __launch_bounds__(C5_T, 5) c5_forward_kernel(const __grid_constant__ C5Params p) {
   __shared__ __align__(128) float xst[2][FX_N];  // x: double-buffered TMA stages
-  __shared__ __align__(16) float us[FY_H * FY_W];
+  __shared__ __align__(16) float us[FY_H * US_W];
   __shared__ f2 m2[C5_MK * C5_MK];
-  __shared__ f2 nl2[C5_BK * C5_BK];
+  __shared__ __align__(16) f2 nl2[C5_BK * NL_W];
   __shared__ __align__(8) uint64_t bars[2];
   double *dsh = reinterpret_cast<double *>(&xst[0][0]);  // the final combine, after the tiles
   const int W = p.w, H = p.h, bm = p.bmode;
@@ -310,7 +325,11 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
     const float m = __ldg(p.mask_dev + i);
     m2[i] = f2_pack(m, m);
   }
-  for (int i = threadIdx.x; i < C5_BK * C5_BK; i += C5_T) nl2[i] = f2_pack(-p.lsm[i], -p.lsm[i]);
+  for (int i = threadIdx.x; i < C5_BK * NL_W; i += C5_T) {
+    const int oy = i / NL_W, ox = i - oy * NL_W;
+    const float n = ox < C5_BK ? -p.lsm[oy * C5_BK + ox] : 0.0f;
+    nl2[i] = f2_pack(n, n);
+  }
   float c, k2;
   sigma_consts(p, c, k2);
   const float q = sqrtf(-k2), inv_q = 1.0f / q;
@@ -321,7 +340,7 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
   auto issue = [&](int tile, int s) {
     int b, X0, Y0;
     tile_origin<F_TW, F_TH>(p, tile, b, X0, Y0);
-    c5_issue(&bars[s], FX_N * 4, xst[s], &p.map_xf, nullptr, nullptr, X0 - 8, Y0 - FX_R, b);
+    c5_issue(&bars[s], FX_W * FX_H * 4, xst[s], &p.map_xf, nullptr, nullptr, X0 - 8, Y0 - FX_R, b);
   };
   if (p.use_tma && threadIdx.x == 0) issue(blockIdx.x, 0);
   int it = 0;
@@ -329,7 +348,7 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
     int b, X0, Y0;
     tile_origin<F_TW, F_TH>(p, tile, b, X0, Y0);
     const float *x = p.x + (int64_t)b * p.xb;
-    const bool edge = !(X0 >= 8 && X0 + F_TW + 8 <= W && Y0 >= FX_R && Y0 + F_TH + FX_R <= H);
+    const bool edge = !(X0 >= 8 && X0 - 8 + FX_W <= W && Y0 >= FX_R && Y0 + F_TH + FX_R <= H);
     float *xs = xst[p.use_tma ? (it & 1) : 0];
     // x on rows Y0-7 .., columns X0-8 .. through the boundary
     if (p.use_tma) {
@@ -342,7 +361,7 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
       }
       if (!c5_wait(p, bars, it, next)) break;
       if (edge) {  // cells outside the image (zero-filled) through the boundary
-        for (int cc = threadIdx.x; cc < FX_N; cc += C5_T) {
+        for (int cc = threadIdx.x; cc < FX_W * FX_H; cc += C5_T) {
           const int r = cc / FX_W, k = cc - r * FX_W;
           const int vy = Y0 - FX_R + r, vx = X0 - 8 + k;
           if (vy >= 0 && vy < H && vx >= 0 && vx < W) continue;
@@ -360,7 +379,7 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
               __ldg(reinterpret_cast<const float4 *>(x + (int64_t)(Y0 - FX_R + r) * p.xp + X0 - 8) + k4);
         }
       } else {
-        for (int cc = threadIdx.x; cc < FX_N; cc += C5_T) {
+        for (int cc = threadIdx.x; cc < FX_W * FX_H; cc += C5_T) {
           const int r = cc / FX_W, k = cc - r * FX_W;
           const int ry = remap_c5(bm, Y0 - FX_R + r, H), rx = remap_c5(bm, X0 - 8 + k, W);
           xs[cc] = (ry == C5_OUT || rx == C5_OUT) ? 0.0f : __ldg(x + (int64_t)ry * p.xp + rx);
@@ -372,7 +391,8 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
     // one 16-value row window of x per mask row, taps row-major (y1 exactly as
     // hgb_local_op computes it)
     if (threadIdx.x < FY_H * (FY_W / 8)) {
-      const int r = threadIdx.x / (FY_W / 8), k0 = (threadIdx.x - r * (FY_W / 8)) * 8;
+      // consecutive threads take consecutive rows (distinct bank groups)
+      const int g = threadIdx.x / FY_H, r = threadIdx.x - g * FY_H, k0 = 8 * g;
       f2 acc[4] = {0ull, 0ull, 0ull, 0ull};
 #pragma unroll
       for (int my = 0; my < C5_MK; ++my) {
@@ -393,7 +413,7 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
           for (int i = 0; i < 4; ++i) acc[i] = f2_fma(M, f2_pack(w[2 * i + 1 + mx], w[2 * i + 2 + mx]), acc[i]);
         }
       }
-      float4 *o = reinterpret_cast<float4 *>(&us[r * FY_W + k0]);
+      float4 *o = reinterpret_cast<float4 *>(&us[r * US_W + k0]);
       o[0] = make_float4(q * f2_lo(acc[0]), q * f2_hi(acc[0]), q * f2_lo(acc[1]), q * f2_hi(acc[1]));
       o[1] = make_float4(q * f2_lo(acc[2]), q * f2_hi(acc[2]), q * f2_lo(acc[3]), q * f2_hi(acc[3]));
     }
@@ -408,17 +428,26 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
         if (vy >= 0 && vy < H && vx >= 0 && vx < W) continue;
         if (vy < -C5_BR || vy >= H + C5_BR || vx < -C5_BR || vx >= W + C5_BR) continue;
         const int ry = remap_c5(bm, vy, H), rx = remap_c5(bm, vx, W);
-        us[cc] = (ry == C5_OUT || rx == C5_OUT) ? 0.0f : us[(ry - Y0 + C5_BR) * FY_W + rx - X0 + C5_BR];
+        us[r * US_W + k] = (ry == C5_OUT || rx == C5_OUT) ? 0.0f : us[(ry - Y0 + C5_BR) * US_W + rx - X0 + C5_BR];
       }
       __syncthreads();
     }
+    // the targets of the four pixels, loaded before the bilateral hides their latency
+    const int gy = Y0 + ty, gx0 = X0 + 4 * tx;
+    float tv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (gy < H) {
+      const float *trow = p.t + (int64_t)b * p.tb + (int64_t)gy * p.tp;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (gx0 + i < W) tv[i] = __ldg(trow + gx0 + i);
+    }
     // bilateral: pixels 4 tx .. 4 tx + 3 of row ty, pairs (0, 1) and (2, 3)
-    const float4 cv = *reinterpret_cast<const float4 *>(&us[(ty + C5_BR) * FY_W + 4 * tx + C5_BR]);
+    const float4 cv = *reinterpret_cast<const float4 *>(&us[(ty + C5_BR) * US_W + 4 * tx + C5_BR]);
     const f2 C0 = f2_pack(cv.x, cv.y), C1 = f2_pack(cv.z, cv.w);
     f2 Ws0 = 0ull, Ws1 = 0ull, Ns0 = 0ull, Ns1 = 0ull;
 #pragma unroll 1
     for (int oy = 0; oy < C5_BK; ++oy) {
-      const float4 *row = reinterpret_cast<const float4 *>(&us[(ty + oy) * FY_W + 4 * tx]);
+      const float4 *row = reinterpret_cast<const float4 *>(&us[(ty + oy) * US_W + 4 * tx]);
       float w[12];
 #pragma unroll
       for (int v = 0; v < 3; ++v) {
@@ -428,26 +457,26 @@ __global__ void __launch_bounds__(C5_T) c5_forward_kernel(const __grid_constant_
         w[4 * v + 2] = t4.z;
         w[4 * v + 3] = t4.w;
       }
+      f2 NLr[NL_W];
+      nl_row(&nl2[oy * NL_W], NLr);
 #pragma unroll
       for (int ox = 0; ox < C5_BK; ++ox) {
-        const f2 NL = nl2[oy * C5_BK + ox];
+        const f2 NL = NLr[ox];
         bil_tap(f2_pack(w[ox], w[ox + 1]), C0, NL, Ws0, Ns0);
         bil_tap(f2_pack(w[ox + 2], w[ox + 3]), C1, NL, Ws1, Ns1);
       }
     }
-    const int gy = Y0 + ty, gx0 = X0 + 4 * tx;
     if (gy < H && gx0 < W) {
       const float Wv[4] = {f2_lo(Ws0), f2_hi(Ws0), f2_lo(Ws1), f2_hi(Ws1)};
       const float Nv[4] = {f2_lo(Ns0), f2_hi(Ns0), f2_lo(Ns1), f2_hi(Ns1)};
       const float Uv[4] = {cv.x, cv.y, cv.z, cv.w};
-      const float *trow = p.t + (int64_t)b * p.tb + (int64_t)gy * p.tp;
       float4 *orow = p.pk + (int64_t)b * p.ib + (int64_t)gy * p.ip;
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const int gx = gx0 + i;
         if (gx >= W) break;
         const float uy = Nv[i] / Wv[i];
-        const float e = uy * inv_q - __ldg(trow + gx);
+        const float e = uy * inv_q - tv[i];
         lsum = kahan_add(lsum, e * e);
         const float a = (g_scale * e) / Wv[i];
         orow[gx] = make_float4(Uv[i], a, -a * uy, uy);
@@ -505,11 +534,13 @@ __device__ float bil_adj_band(const C5Params &p, const float4 *pk, int jy, int j
     for (int oy = 0; oy < C5_BK; ++oy) {
       const int py = pry[iy] - (oy - C5_BR);
       if (py < 0 || py >= H) continue;
+      const float4 *prow = pk + (int64_t)py * p.ip;
       for (int ix = 0; ix < nx; ++ix)
-        for (int ox = 0; ox < C5_BK; ++ox) {
+#pragma unroll
+        for (int ox = 0; ox < C5_BK; ++ox) {  // the row's loads in flight together
           const int px = prx[ix] - (ox - C5_BR);
           if (px < 0 || px >= W) continue;
-          const float4 P = __ldg(pk + (int64_t)py * p.ip + px);
+          const float4 P = __ldg(prow + px);
           const float d = J.x - P.x;
           const float e = ex2f(__fmaf_rn(-d, d, lsm[oy * C5_BK + ox]));
           dn = __fmaf_rn(e, __fmaf_rn(-C2S * d, __fmaf_rn(J.x, P.y, P.z), P.y), dn);
@@ -523,14 +554,16 @@ __global__ void __launch_bounds__(C5_T, 4) c5_bilateral_adjoint_kernel(const __g
   // so that a pixel pair's neighbours at any offset are one aligned load each
   __shared__ __align__(16) float4 sq[FY_H * SQ_W];
   __shared__ __align__(16) f2 sb[FY_H * SB_W];
-  __shared__ f2 nl2[C5_BK * C5_BK];
+  __shared__ __align__(16) f2 nl2[C5_BK * NL_W];
   __shared__ float lsm[C5_BK * C5_BK];
   __shared__ float sbuf[32];
   double *dsh = reinterpret_cast<double *>(sq);  // the final combine, after the tiles
   const int W = p.w, H = p.h;
-  for (int i = threadIdx.x; i < C5_BK * C5_BK; i += C5_T) {
-    lsm[i] = p.lsm[i];
-    nl2[i] = f2_pack(-p.lsm[i], -p.lsm[i]);
+  for (int i = threadIdx.x; i < C5_BK * NL_W; i += C5_T) {
+    const int oy = i / NL_W, ox = i - oy * NL_W;
+    const float n = ox < C5_BK ? -p.lsm[oy * C5_BK + ox] : 0.0f;
+    nl2[i] = f2_pack(n, n);
+    if (ox < C5_BK) lsm[oy * C5_BK + ox] = p.lsm[oy * C5_BK + ox];
   }
   float c, k2;
   sigma_consts(p, c, k2);
@@ -577,9 +610,8 @@ __global__ void __launch_bounds__(C5_T, 4) c5_bilateral_adjoint_kernel(const __g
         const int row = ty + 2 * C5_BR - oy;
         const float4 *qr = &sq[row * SQ_W + qbase];
         const f2 *br = &sb[row * SB_W + bbase];
-        f2 NL[C5_BK];
-#pragma unroll
-        for (int ox = 0; ox < C5_BK; ++ox) NL[ox] = nl2[oy * C5_BK + ox];
+        f2 NL[NL_W];
+        nl_row(&nl2[oy * NL_W], NL);
 #pragma unroll
         for (int s = 0; s <= 2 * C5_BR + 2; ++s) {
           const float4 P = qr[s + (s < 4 ? 0 : s < 8 ? q1 : 1)];
@@ -664,7 +696,6 @@ __global__ void __launch_bounds__(C5_T, 2) c5_conv_adjoint_kernel(const __grid_c
   __shared__ float msk[C5_MK * C5_MK];
   __shared__ float red[C5_T / 32][C5_MK * C5_MK];
   __shared__ __align__(8) uint64_t bars[2];
-  double *dsh = reinterpret_cast<double *>(&stg[0][0][0]);  // the final combine, after the tiles
   const int W = p.w, H = p.h, bm = p.bmode;
   for (int i = threadIdx.x; i < C5_MK * 8; i += C5_T) {
     const int oy = i / 8, ox = i - oy * 8;
@@ -703,11 +734,13 @@ __global__ void __launch_bounds__(C5_T, 2) c5_conv_adjoint_kernel(const __grid_c
       for (int oy = 0; oy < C5_MK; ++oy) {
         const int sy = pry[iy] - (oy - C5_MR);
         if (sy < 0 || sy >= H) continue;
+        const float *grow = g + (int64_t)sy * p.ip;
         for (int ix = 0; ix < nx; ++ix)
-          for (int ox = 0; ox < C5_MK; ++ox) {
+#pragma unroll
+          for (int ox = 0; ox < C5_MK; ++ox) {  // the row's loads in flight together
             const int sxp = prx[ix] - (ox - C5_MR);
             if (sxp < 0 || sxp >= W) continue;
-            acc = __fmaf_rn(msk[oy * C5_MK + ox], g[(int64_t)sy * p.ip + sxp], acc);
+            acc = __fmaf_rn(msk[oy * C5_MK + ox], grow[sxp], acc);
           }
       }
     p.dx[(int64_t)b * p.dxb + (int64_t)jy * p.dxp + jx] = acc;
@@ -833,10 +866,15 @@ __global__ void __launch_bounds__(C5_T, 2) c5_conv_adjoint_kernel(const __grid_c
     __threadfence();
   }
   if (take_last_ticket(p.tickets + 2)) {
-    for (int o = 0; o < C5_MK * C5_MK; ++o) {
-      const double sum = block_sum_fixed(
-          (int)nb, [&](int i) { return (double)__ldcg(p.dm_part + (size_t)i * C5_MK * C5_MK + o); }, dsh);
-      if (threadIdx.x == 0) p.grad_mask_dev[o] = (float)sum;
+    // a warp per tap: lanes fold the partials i = lane, lane + 32, ... in
+    // order, then a fixed shuffle tree (the same sum on every run)
+    const int wv = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int o = wv; o < C5_MK * C5_MK; o += C5_T / 32) {
+      double sum = 0.0;
+      for (int i = lane; i < (int)nb; i += 32) sum += (double)__ldcg(p.dm_part + (size_t)i * C5_MK * C5_MK + o);
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, d);
+      if (lane == 0) p.grad_mask_dev[o] = (float)sum;
     }
     if (threadIdx.x == 0) p.tickets[2] = 0u;
   }
