@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(C5_T, 5) c5_forward_kernel(const __grid_consta
     const float4 cv = *reinterpret_cast<const float4 *>(&us[(ty + C5_BR) * US_W + 4 * tx + C5_BR]);
     const f2 C0 = f2_pack(cv.x, cv.y), C1 = f2_pack(cv.z, cv.w);
     f2 Ws0 = 0ull, Ws1 = 0ull, Ns0 = 0ull, Ns1 = 0ull;
-#pragma unroll 1
+#pragma unroll 3
     for (int oy = 0; oy < C5_BK; ++oy) {
       const float4 *row = reinterpret_cast<const float4 *>(&us[(ty + oy) * US_W + 4 * tx]);
       float w[12];
@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(C5_T, 4) c5_bilateral_adjoint_kernel(const __g
       const f2 A0 = f2_pack(J0.z, J0.w), A1 = f2_pack(J1.z, J1.w);
       const f2 B0 = sb[ce_b + 4], B1 = sb[ce_b + 6];
       f2 s0[4] = {0ull, 0ull, 0ull, 0ull}, s1[4] = {0ull, 0ull, 0ull, 0ull};
-#pragma unroll 1
+#pragma unroll 3
       for (int oy = 0; oy < C5_BK; ++oy) {
         // neighbours p = j - o: row ty + 8 - oy, positions 4 tx + s, s = 0 .. 10;
         // pair 0 takes tap ox = 8 - s, pair 1 tap ox = 10 - s
