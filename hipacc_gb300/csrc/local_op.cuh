@@ -66,7 +66,13 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
   static_assert(TW % VI == 0 && SW % 4 == 0 && PX % 4 == 0, "tile shape");
   constexpr bool kTma = std::is_same<TI, float>::value || std::is_same<TI, uint8_t>::value;
   constexpr bool kU8 = std::is_same<TI, uint8_t>::value;
-  __shared__ __align__(128) float tile[SH * SW];
+  // The FP32 tile the stencil reads.  u8: only the columns the taps reach
+  // (halos rounded to 4), while the byte box keeps 16-byte aligned halos
+  // for TMA; the narrower tile leaves room for more CTAs per SM.
+  constexpr int HLF = kU8 ? round_up(RX, 4) : HL;
+  constexpr int SWF = kU8 ? HLF + TW + round_up(MW - 1 - RX, 4) : SW;
+  static_assert(SWF % 4 == 0 && (HL - HLF) % 4 == 0, "u8 tile shape");
+  __shared__ __align__(128) float tile[SH * SWF];
   // u8: the TMA box lands here as bytes and is widened into `tile`
   __shared__ __align__(128) uint8_t raw[kU8 ? SH * SW : 16];
   __shared__ __align__(8) uint64_t bar;
@@ -100,8 +106,9 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
       // widen 4 bytes at a time: a byte b placed in the mantissa of 2^23 gives
       // 2^23 + b exactly, and subtracting 2^23 leaves b
       const f2 k23 = f2_pack(8388608.0f, 8388608.0f);
-      for (int c = threadIdx.x; c < SH * SW / 4; c += NT) {
-        const uint32_t w = reinterpret_cast<const uint32_t *>(raw)[c];
+      for (int c = threadIdx.x; c < SH * SWF / 4; c += NT) {
+        const int r = c / (SWF / 4), q4 = c - r * (SWF / 4);
+        const uint32_t w = reinterpret_cast<const uint32_t *>(raw + r * SW + (HL - HLF))[q4];
         const f2 lo = f2_sub(f2_pack(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440)),
                                      __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7441))), k23);
         const f2 hi = f2_sub(f2_pack(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7442)),
@@ -111,75 +118,89 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
       if (!interior) __syncthreads();  // the patch below overwrites widened cells
     }
     if (!interior) {
-      // cells outside the image (zero-filled by TMA): left / right columns, top / bottom rows
-      const int nl = max(0, min(SW, ax_lo - X0)), rs = max(0, min(SW, ax_hi - X0));
+      // cells outside the image (zero-filled by TMA): left / right columns, top
+      // / bottom rows of the FP32 tile (its columns start at X0 + HL - HLF)
+      const int XF = X0 + (HL - HLF);
+      const int nl = max(0, min(SWF, ax_lo - XF)), rs = max(0, min(SWF, ax_hi - XF));
       const int nt = max(0, min(SH, ay_lo - Y0)), bs = max(0, min(SH, ay_hi - Y0));
-      const int ncl = nl * SH, ncr = (SW - rs) * SH, nrt = nt * SW, nrb = (SH - bs) * SW;
+      const int ncl = nl * SH, ncr = (SWF - rs) * SH, nrt = nt * SWF, nrb = (SH - bs) * SWF;
       for (int c = threadIdx.x; c < ncl + ncr + nrt + nrb; c += NT) {
         int r, q;
         if (c < ncl) {
           r = c / nl;
           q = c - r * nl;
         } else if (c < ncl + ncr) {
-          const int d = c - ncl, n = SW - rs;
+          const int d = c - ncl, n = SWF - rs;
           r = d / n;
           q = rs + (d - r * n);
         } else if (c < ncl + ncr + nrt) {
           const int d = c - ncl - ncr;
-          r = d / SW;
-          q = d - r * SW;
+          r = d / SWF;
+          q = d - r * SWF;
         } else {
           const int d = c - ncl - ncr - nrt;
-          const int rr = d / SW;
+          const int rr = d / SWF;
           r = bs + rr;
-          q = d - rr * SW;
+          q = d - rr * SWF;
         }
-        const int ry = remap(p.bmode, Y0 + r, ay_lo, ay_hi), rx = remap(p.bmode, X0 + q, ax_lo, ax_hi);
-        tile[r * SW + q] = (ry == (int)0x80000000 || rx == (int)0x80000000)
+        const int ry = remap(p.bmode, Y0 + r, ay_lo, ay_hi), rx = remap(p.bmode, XF + q, ax_lo, ax_hi);
+        tile[r * SWF + q] = (ry == (int)0x80000000 || rx == (int)0x80000000)
                                ? p.cval
                                : Storage<TI>::load(reinterpret_cast<const TI *>(in + (int64_t)ry * p.in_pitch) + rx);
       }
     }
-  } else if (interior && p.vec_in) {
-#pragma unroll 4
-    for (int c = threadIdx.x; c < SH * CPR; c += NT) {
-      const int r = c / CPR, k = c - r * CPR;
-      const TI *src = reinterpret_cast<const TI *>(in + (int64_t)(Y0 + r) * p.in_pitch) + X0 + k * VI;
-      float f[VI];
-      Vec16<TI>::unpack(ldg16(src), f);
-      float *dst = &tile[r * SW + k * VI];
-#pragma unroll
-      for (int q = 0; q < VI; q += 4) *reinterpret_cast<float4 *>(dst + q) = make_float4(f[q], f[q + 1], f[q + 2], f[q + 3]);
+  } else if constexpr (kU8) {
+    // u8 without TMA: bytes through the boundary rule straight into the FP32 tile
+    const int XF = X0 + (HL - HLF);
+    for (int c = threadIdx.x; c < SH * SWF; c += NT) {
+      const int r = c / SWF, q = c - r * SWF;
+      const int ry = remap(p.bmode, Y0 + r, ay_lo, ay_hi), rx = remap(p.bmode, XF + q, ax_lo, ax_hi);
+      tile[c] = (ry == (int)0x80000000 || rx == (int)0x80000000)
+                    ? p.cval
+                    : Storage<TI>::load(reinterpret_cast<const TI *>(in + (int64_t)ry * p.in_pitch) + rx);
     }
   } else {
-    for (int c = threadIdx.x; c < SH * CPR; c += NT) {
-      const int r = c / CPR, k = c - r * CPR;
-      const int ay = Y0 + r, ax0 = X0 + k * VI;
-      float f[VI];
-      if (p.vec_in && ay >= ay_lo && ay < ay_hi && ax0 >= ax_lo && ax0 + VI <= ax_hi) {
-        const TI *src = reinterpret_cast<const TI *>(in + (int64_t)ay * p.in_pitch) + ax0;
+    if (interior && p.vec_in) {
+#pragma unroll 4
+      for (int c = threadIdx.x; c < SH * CPR; c += NT) {
+        const int r = c / CPR, k = c - r * CPR;
+        const TI *src = reinterpret_cast<const TI *>(in + (int64_t)(Y0 + r) * p.in_pitch) + X0 + k * VI;
+        float f[VI];
         Vec16<TI>::unpack(ldg16(src), f);
-      } else {
-        const int ry = remap(p.bmode, ay, ay_lo, ay_hi);
-        const TI *row = reinterpret_cast<const TI *>(in + (int64_t)(ry == (int)0x80000000 ? ay_lo : ry) * p.in_pitch);
+        float *dst = &tile[r * SW + k * VI];
 #pragma unroll
-        for (int q = 0; q < VI; ++q) {
-          const int rx = remap(p.bmode, ax0 + q, ax_lo, ax_hi);
-          f[q] = (rx == (int)0x80000000 || ry == (int)0x80000000) ? p.cval : Storage<TI>::load(row + rx);
-        }
+        for (int q = 0; q < VI; q += 4) *reinterpret_cast<float4 *>(dst + q) = make_float4(f[q], f[q + 1], f[q + 2], f[q + 3]);
       }
-      float *dst = &tile[r * SW + k * VI];
+    } else {
+      for (int c = threadIdx.x; c < SH * CPR; c += NT) {
+        const int r = c / CPR, k = c - r * CPR;
+        const int ay = Y0 + r, ax0 = X0 + k * VI;
+        float f[VI];
+        if (p.vec_in && ay >= ay_lo && ay < ay_hi && ax0 >= ax_lo && ax0 + VI <= ax_hi) {
+          const TI *src = reinterpret_cast<const TI *>(in + (int64_t)ay * p.in_pitch) + ax0;
+          Vec16<TI>::unpack(ldg16(src), f);
+        } else {
+          const int ry = remap(p.bmode, ay, ay_lo, ay_hi);
+          const TI *row = reinterpret_cast<const TI *>(in + (int64_t)(ry == (int)0x80000000 ? ay_lo : ry) * p.in_pitch);
 #pragma unroll
-      for (int q = 0; q < VI; q += 4) *reinterpret_cast<float4 *>(dst + q) = make_float4(f[q], f[q + 1], f[q + 2], f[q + 3]);
+          for (int q = 0; q < VI; ++q) {
+            const int rx = remap(p.bmode, ax0 + q, ax_lo, ax_hi);
+            f[q] = (rx == (int)0x80000000 || ry == (int)0x80000000) ? p.cval : Storage<TI>::load(row + rx);
+          }
+        }
+        float *dst = &tile[r * SW + k * VI];
+#pragma unroll
+        for (int q = 0; q < VI; q += 4) *reinterpret_cast<float4 *>(dst + q) = make_float4(f[q], f[q + 1], f[q + 2], f[q + 3]);
+      }
     }
   }
   __syncthreads();
 
   // ---- register-blocked stencil
   const int tx = threadIdx.x % BX, ty = threadIdx.x / BX;
-  constexpr int OFF = (HL - RX) % 4;
+  constexpr int OFF = (HLF - RX) % 4;
   constexpr int NV = cdiv(OFF + PX + MW - 1, 4);
-  const int cbase = HL - RX - OFF + tx * PX;
+  const int cbase = HLF - RX - OFF + tx * PX;
   constexpr int NP = PX / 2;
   f2 acc2[PY][NP];
 #pragma unroll
@@ -190,7 +211,7 @@ __global__ void __launch_bounds__(BX *BY) conv_kernel(const __grid_constant__ Co
 #pragma unroll
   for (int r = 0; r < PY + MH - 1; ++r) {
     float win[NV * 4];
-    const float *row = &tile[(ty * PY + r) * SW + cbase];
+    const float *row = &tile[(ty * PY + r) * SWF + cbase];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       const float4 t = *reinterpret_cast<const float4 *>(row + 4 * v);
