@@ -141,6 +141,52 @@ __global__ void __launch_bounds__(HB_T) hist_kernel(const __grid_constant__ Hist
   }
 }
 
+// u8 pixels, identity table, dense rows, 16-byte loads: one flat run of n
+// bytes.  Every byte goes to lane column slot v (256 slots; the slots from
+// lim on, which the table sends past the last bin, are never published), so
+// a pixel costs a byte extract, an address and one shared-memory atomic.
+// (Per-thread 16-bit counter columns updated by plain load / add / store
+// measured slower, 22.8 against 15.7 us on 4096^2: each update waits for the
+// previous one of the same thread, and 64 KB per CTA leaves 12 warps per SM.)
+__global__ void __launch_bounds__(HB_T) hist_u8_direct_kernel(const __grid_constant__ HistParams p, int64_t n) {
+  __shared__ uint32_t h[256 * 32];
+  for (int i = threadIdx.x; i < 256 * 32; i += HB_T) h[i] = 0u;
+  __syncthreads();
+  const unsigned lane = threadIdx.x & 31;
+  uint32_t *hl = h + lane;
+  const uint8_t *src = reinterpret_cast<const uint8_t *>(p.in) + ((int64_t)p.oy * p.pitch + p.ox);
+  const int64_t nchunks = n >> 4;
+  const int64_t stride = (int64_t)gridDim.x * HB_T;
+  constexpr int U = 4;  // chunks in flight per thread
+  auto count = [&](uint32_t w) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) atomicAdd(hl + (__byte_perm(w, 0u, 0x4440 + k) << 5), 1u);
+  };
+  for (int64_t c0 = (int64_t)blockIdx.x * HB_T + threadIdx.x; c0 < nchunks; c0 += U * stride) {
+    uint4 v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (c0 + u * stride < nchunks) v[u] = ldg16(src + 16 * (c0 + u * stride));
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (c0 + u * stride < nchunks) {
+        count(v[u].x);
+        count(v[u].y);
+        count(v[u].z);
+        count(v[u].w);
+      }
+  }
+  // the last n mod 16 bytes: block 0
+  if (blockIdx.x == 0)
+    for (int64_t i = (nchunks << 4) + threadIdx.x; i < n; i += HB_T) atomicAdd(hl + ((uint32_t)src[i] << 5), 1u);
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < p.lim && i < p.nb; i += HB_T) {
+    uint32_t c = 0;
+    for (int k = 0; k < 32; ++k) c += h[(i << 5) | ((k + i) & 31)];  // rotate to spread banks
+    if (c) atomicAdd(&p.bins[i], c);
+  }
+}
+
 }  // namespace
 }  // namespace hgb
 
@@ -206,6 +252,21 @@ extern "C" int hgb_histogram(const hgb_view *in, const hgb_window *win, unsigned
   const size_t copies = p.layout == 2 ? 32 : (p.layout == 1 ? HB_T / 32 : 1);
   const size_t smem = ((size_t)num_bins * copies + (in->dtype == HGB_U8 && !p.direct ? 256 * 32 : 0)) * 4;
   HGB_CHECK_CUDA(cudaMemsetAsync(bins, 0, (size_t)num_bins * 4, st));
+  if (in->dtype == HGB_U8 && p.direct && p.dense && p.vec) {
+    const int64_t n = (int64_t)w.width * w.height * in->batch;
+    const int per_sm = resident_ctas((const void *)hist_u8_direct_kernel, HB_T, 0);
+    const int grid =
+        (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)num_sms() * per_sm, (n / 16 + HB_T - 1) / HB_T));
+    cudaEvent_t ev = before_launch(st);
+    hist_u8_direct_kernel<<<grid, HB_T, 0, st>>>(p, n);
+    rc = after_launch("hist_u8_direct_kernel", st, ev);
+    if (rc) return rc;
+    if (bins_host) {
+      HGB_CHECK_CUDA(cudaMemcpyAsync(bins_host, bins, (size_t)num_bins * 4, cudaMemcpyDeviceToHost, st));
+      HGB_CHECK_CUDA(cudaStreamSynchronize(st));
+    }
+    return HGB_OK;
+  }
   const void *kern = in->dtype == HGB_U8 ? (const void *)hist_kernel<uint8_t> : (const void *)hist_kernel<float>;
   rc = ensure_dynamic_smem(kern, smem);
   if (rc) return rc;
