@@ -57,6 +57,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "band.cuh"
 #include "reduce_common.cuh"
 #include "tma.cuh"
 
@@ -182,54 +183,6 @@ __device__ __forceinline__ float block_sum_f(float v, float *sbuf) {
     for (int i = 0; i < C5_T / 32; ++i) r += sbuf[i];
   __syncthreads();
   return r;
-}
-
-// per-axis pre-images of index j under the remap, among virtual positions
-// within `rad` of the image: at most 1 + rad entries
-__device__ __forceinline__ int preimages(int mode, int j, int n, int rad, int *out) {
-  int k = 0;
-  out[k++] = j;
-  if (mode == HGB_BOUNDARY_CONSTANT || (j >= rad && j < n - rad)) return k;
-  for (int v = -rad; v < 0; ++v)
-    if (remap(mode, v, 0, n) == j) out[k++] = v;
-  for (int v = n; v < n + rad; ++v)
-    if (remap(mode, v, 0, n) == j) out[k++] = v;
-  return k;
-}
-
-// Band of radius R along the edges of a W x H image, as the pixels that the
-// tile paths leave out: rows [0, R) and [H-R, H) whole, then for the rows in
-// between columns [0, 4) and [W-wr, W), wr = W - 4 floor((W - R) / 4) (the
-// tile paths take groups of four columns whose taps all stay inside).
-__host__ __device__ __forceinline__ int band_right(int W, int R) { return W - 4 * ((W - R) / 4); }
-__host__ __device__ __forceinline__ int band_size(int W, int H, int R) {
-  return 2 * R * W + (H - 2 * R) * (4 + band_right(W, R));
-}
-__device__ __forceinline__ void band_pos(int k, int W, int H, int R, int &y, int &x) {
-  if (k < 2 * R * W) {
-    const int yy = k / W;
-    x = k - yy * W;
-    y = yy < R ? yy : H - 2 * R + yy;
-    return;
-  }
-  k -= 2 * R * W;
-  const int mid = (H - 2 * R) * 4;
-  if (k < mid) {
-    y = R + (k >> 2);
-    x = k & 3;
-    return;
-  }
-  k -= mid;
-  const int wr = band_right(W, R);
-  const int yy = k / wr;
-  y = R + yy;
-  x = W - wr + (k - yy * wr);
-}
-
-// the contiguous share of n band entries that this CTA takes
-__device__ __forceinline__ void cta_share(int64_t n, int64_t &k0, int64_t &k1) {
-  k0 = n * blockIdx.x / gridDim.x;
-  k1 = n * (blockIdx.x + 1) / gridDim.x;
 }
 
 // per-CTA Kahan partial of the squared error, FP64 combine by the last CTA

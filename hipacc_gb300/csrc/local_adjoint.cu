@@ -11,9 +11,20 @@
 // (CLAMP: all positions beyond the edge, MIRROR: the reflected one, REPEAT: the
 // wrapped ones).  grad_m is reduced per tap over row blocks and combined in
 // FP64 in a fixed order, so it is deterministic.  FP32 storage.
+//
+// Both gradients of a square 3x3, 5x5 or 7x7 mask on TMA-legal images of at
+// least 8 x 8 go through one fused persistent kernel (adj_fused_kernel): the
+// CTA walks 64 x 16 tiles, stages grad_out and in with TMA into two buffers
+// (the next tile's boxes land while this one computes), reads twelve-value
+// register windows per row, and accumulates the mask gradient per pair of taps
+// in packed f32x2 registers; pixels within the mask radius of an edge go
+// through the pre-images from a flat band list after the tiles.
+#include <algorithm>
 #include <cstring>
 
+#include "band.cuh"
 #include "reduce_common.cuh"
+#include "tma.cuh"
 
 namespace hgb {
 namespace {
@@ -249,6 +260,220 @@ __global__ void __launch_bounds__(LA_T) adj_mask_tile_kernel(const __grid_consta
   }
 }
 
+// ---------------------------------------------------------------- fused form
+constexpr int AF_TW = 64, AF_TH = 16, AF_GX = AF_TW / 4, AF_W = AF_TW + 8;  // staged columns X0-4 ..
+
+struct AdjFusedParams {
+  CUtensorMap map_g;  // grad_out, box AF_W x (AF_TH + 2R)
+  CUtensorMap map_x;  // in, same box
+  AdjParams p;
+  int *status;
+  int tiles_x, tiles_y, ntiles;
+  int vec_gin;        // grad_in rows allow aligned 16-byte stores
+};
+
+template <int K>
+struct AfShape {
+  static constexpr int R = K / 2, H = AF_TH + 2 * R, NP = (K + 1) / 2;  // staged rows, tap pairs per mask row
+  static constexpr int N = (AF_W * H + 31) / 32 * 32;                   // floats per staged array (128-byte multiple)
+};
+
+__device__ __forceinline__ void af_window12(const float *row, float (&w)[12]) {
+#pragma unroll
+  for (int v = 0; v < 3; ++v) {
+    const float4 t4 = reinterpret_cast<const float4 *>(row)[v];
+    w[4 * v] = t4.x;
+    w[4 * v + 1] = t4.y;
+    w[4 * v + 2] = t4.z;
+    w[4 * v + 3] = t4.w;
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(LA_T, 2) adj_fused_kernel(const __grid_constant__ AdjFusedParams P) {
+  using S = AfShape<K>;
+  constexpr int R = S::R, FH = S::H, NP = S::NP, FN = S::N;
+  static_assert(R <= 3, "the twelve-value windows cover radius 3");
+  __shared__ __align__(128) float stg[2][2][FN];  // [buffer][grad_out, in]
+  __shared__ __align__(16) f2 m2[K][2 * NP];     // mask pairs (m, m), padded to an even count per row
+  __shared__ float msk[K * K];
+  __shared__ float red[LA_T / 32][K * K];
+  __shared__ __align__(8) uint64_t bars[2];
+  const AdjParams &p = P.p;
+  const int W = p.w, H = p.h, bm = p.bmode;
+  for (int i = threadIdx.x; i < K * 2 * NP; i += LA_T) {
+    const int oy = i / (2 * NP), ox = i - oy * (2 * NP);
+    const float m = ox < K ? (p.mask_dev ? __ldg(p.mask_dev + oy * K + ox) : p.mask[oy * K + ox]) : 0.0f;
+    m2[oy][ox] = f2_pack(m, m);
+    if (ox < K) msk[oy * K + ox] = m;
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  auto origin = [&](int t, int &b, int &X0, int &Y0) {
+    const int per = P.tiles_x * P.tiles_y, bz = t / per, r = t - bz * per, by = r / P.tiles_x;
+    b = bz;
+    X0 = (r - by * P.tiles_x) * AF_TW;
+    Y0 = by * AF_TH;
+  };
+  auto issue = [&](int t, int s) {
+    int b, X0, Y0;
+    origin(t, b, X0, Y0);
+    mbar_expect_tx(&bars[s], 2 * AF_W * FH * 4);
+    tma_load_3d(stg[s][0], &P.map_g, X0 - 4, Y0 - R, b, &bars[s]);
+    tma_load_3d(stg[s][1], &P.map_x, X0 - 4, Y0 - R, b, &bars[s]);
+  };
+  // the first tile's boxes land while the band's grad_in runs
+  if (threadIdx.x == 0) issue(blockIdx.x, 0);
+  const int band_per = band_size(W, H, R);
+  int64_t k0, k1;
+  cta_share((int64_t)band_per * p.batch, k0, k1);
+  for (int64_t k = k0 + threadIdx.x; k < k1; k += LA_T) {
+    const int b = (int)(k / band_per);
+    int jy, jx;
+    band_pos((int)(k - (int64_t)b * band_per), W, H, R, jy, jx);
+    const float *g = p.gout + (int64_t)b * p.gout_b;
+    int prx[1 + R], pry[1 + R];
+    const int nx = preimages(bm, jx, W, R, prx), ny = preimages(bm, jy, H, R, pry);
+    float acc = 0.0f;
+    for (int iy = 0; iy < ny; ++iy)
+      for (int oy = 0; oy < K; ++oy) {
+        const int sy = pry[iy] - (oy - R);
+        if (sy < 0 || sy >= H) continue;
+        const float *grow = g + (int64_t)sy * p.gout_p;
+        for (int ix = 0; ix < nx; ++ix)
+#pragma unroll
+          for (int ox = 0; ox < K; ++ox) {  // the row's loads in flight together
+            const int sxp = prx[ix] - (ox - R);
+            if (sxp < 0 || sxp >= W) continue;
+            acc = __fmaf_rn(msk[oy * K + ox], grow[sxp], acc);
+          }
+      }
+    p.gin[(int64_t)b * p.gin_b + (int64_t)jy * p.gin_p + jx] = acc;
+  }
+  const int tx = threadIdx.x % AF_GX, ty = threadIdx.x / AF_GX;
+  f2 DM[K][NP];  // dL/dmask per pair of taps (oy, 2 op), (oy, 2 op + 1)
+#pragma unroll
+  for (int i = 0; i < K; ++i)
+#pragma unroll
+    for (int j = 0; j < NP; ++j) DM[i][j] = 0ull;
+  int it = 0;
+  for (int t = blockIdx.x; t < P.ntiles; t += gridDim.x, ++it) {
+    int b, X0, Y0;
+    origin(t, b, X0, Y0);
+    const int s = it & 1;
+    // the next tile's boxes land while this one computes
+    const bool next = t + (int)gridDim.x < P.ntiles;
+    if (next && threadIdx.x == 0) {
+      fence_proxy_async_smem();
+      issue(t + gridDim.x, s ^ 1);
+    }
+    if (!cta_wait(&bars[s], (it >> 1) & 1)) {
+      if (threadIdx.x == 0) {
+        record_status(P.status, HGB_ERR_TIMEOUT);
+        mbar_wait(&bars[s], (it >> 1) & 1);
+        if (next) mbar_wait(&bars[s ^ 1], ((it + 1) >> 1) & 1);
+      }
+      break;
+    }
+    const float *sg = stg[s][0], *sx = stg[s][1];
+    const int jx0 = X0 + 4 * tx, jy = Y0 + ty;
+    if (jx0 >= 4 && jx0 + 3 < W - R && jy >= R && jy < H - R) {
+      // grad_in: pixel pair pp (staged column 4 tx + 4 + 2 pp) gathers
+      // grad_out at columns 4 tx + 4 + 2 pp + R - ox of row ty + 2R - oy
+      f2 GI0 = 0ull, GI1 = 0ull;
+#pragma unroll
+      for (int oy = 0; oy < K; ++oy) {
+        float w[12];
+        af_window12(&sg[(ty + 2 * R - oy) * AF_W + 4 * tx], w);
+        const float4 *mr = reinterpret_cast<const float4 *>(&m2[oy][0]);
+#pragma unroll
+        for (int o2 = 0; o2 < NP; ++o2) {
+          const float4 mm = mr[o2];  // taps 2 o2, 2 o2 + 1 as pairs (m, m)
+#pragma unroll
+          for (int l = 0; l < 2; ++l) {
+            const int ox = 2 * o2 + l;
+            if (ox >= K) continue;
+            const f2 M = l ? f2_pack(mm.z, mm.w) : f2_pack(mm.x, mm.y);
+            GI0 = f2_fma(M, f2_pack(w[4 + R - ox], w[5 + R - ox]), GI0);
+            GI1 = f2_fma(M, f2_pack(w[6 + R - ox], w[7 + R - ox]), GI1);
+          }
+        }
+      }
+      float *dxr = p.gin + (int64_t)b * p.gin_b + (int64_t)jy * p.gin_p + jx0;
+      if (P.vec_gin) {
+        *reinterpret_cast<float4 *>(dxr) = make_float4(f2_lo(GI0), f2_hi(GI0), f2_lo(GI1), f2_hi(GI1));
+      } else {
+        dxr[0] = f2_lo(GI0);
+        dxr[1] = f2_hi(GI0);
+        dxr[2] = f2_lo(GI1);
+        dxr[3] = f2_hi(GI1);
+      }
+      // mask gradient: pixel i (column 4 tx + 4 + i) with in at columns
+      // 4 tx + 4 + i - R + ox of row ty + oy
+      const float4 gc = *reinterpret_cast<const float4 *>(&sg[(ty + R) * AF_W + 4 * tx + 4]);
+      const f2 GG[4] = {f2_pack(gc.x, gc.x), f2_pack(gc.y, gc.y), f2_pack(gc.z, gc.z), f2_pack(gc.w, gc.w)};
+#pragma unroll
+      for (int oy = 0; oy < K; ++oy) {
+        float xw[12];
+        af_window12(&sx[(ty + oy) * AF_W + 4 * tx], xw);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int op = 0; op < NP; ++op)
+            DM[oy][op] = f2_fma(GG[i], f2_pack(xw[4 - R + i + 2 * op], xw[5 - R + i + 2 * op]), DM[oy][op]);
+      }
+    }
+    __syncthreads();  // every thread is done with this buffer before it is reloaded
+  }
+  // band pixels, second part: their mask-gradient terms (in through the boundary;
+  // CONSTANT taps outside carry none)
+  for (int64_t k = k0 + threadIdx.x; k < k1; k += LA_T) {
+    const int b = (int)(k / band_per);
+    int jy, jx;
+    band_pos((int)(k - (int64_t)b * band_per), W, H, R, jy, jx);
+    const float gj = p.gout[(int64_t)b * p.gout_b + (int64_t)jy * p.gout_p + jx];
+    const float *x = p.in + (int64_t)b * p.in_b;
+    const f2 GJ = f2_pack(gj, gj);
+    int rx[2 * NP];
+#pragma unroll
+    for (int o = 0; o < 2 * NP; ++o) rx[o] = o < K ? remap(bm, jx + o - R, 0, W) : (int)0x80000000;
+#pragma unroll
+    for (int oy = 0; oy < K; ++oy) {
+      const int ry = remap(bm, jy + oy - R, 0, H);
+#pragma unroll
+      for (int op = 0; op < NP; ++op) {
+        const float x0 = (ry == (int)0x80000000 || rx[2 * op] == (int)0x80000000)
+                             ? 0.0f
+                             : __ldg(x + (int64_t)ry * p.in_p + rx[2 * op]);
+        const float x1 = (ry == (int)0x80000000 || rx[2 * op + 1] == (int)0x80000000)
+                             ? 0.0f
+                             : __ldg(x + (int64_t)ry * p.in_p + rx[2 * op + 1]);
+        DM[oy][op] = f2_fma(GJ, f2_pack(x0, x1), DM[oy][op]);
+      }
+    }
+  }
+  // per-CTA partial of every tap: warp sums, then the warps in order
+#pragma unroll
+  for (int oy = 0; oy < K; ++oy)
+#pragma unroll
+    for (int ox = 0; ox < K; ++ox) {
+      float v = (ox & 1) ? f2_hi(DM[oy][ox >> 1]) : f2_lo(DM[oy][ox >> 1]);
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][oy * K + ox] = v;
+    }
+  __syncthreads();
+  for (int o = threadIdx.x; o < K * K; o += LA_T) {
+    float sum = 0.0f;
+    for (int wv = 0; wv < LA_T / 32; ++wv) sum += red[wv][o];
+    p.part[(size_t)o * gridDim.x + blockIdx.x] = sum;
+  }
+}
+
 // one CTA per tap: thread t folds partials t, t + LA_T, ... in FP64, then a
 // fixed tree over the threads (the same order on every run)
 __global__ void __launch_bounds__(LA_T) adj_mask_combine(const __grid_constant__ AdjParams p, int nparts) {
@@ -321,6 +546,44 @@ extern "C" int hgb_local_op_adjoint(const hgb_view *in, const hgb_view *grad_out
     for (int i = 0; i < mask_w * mask_h; ++i) p.mask[i] = mask[i];
   p.grad_mask_dev = grad_mask_dev;
   cudaStream_t st = (cudaStream_t)stream;
+  const int K = mask_w;
+  if (grad_in && grad_mask_dev && mask_w == mask_h && (K == 3 || K == 5 || K == 7) && p.w >= 8 && p.h >= 8 &&
+      tma_legal(p.gout, grad_out->pitch, grad_out->batch_stride, p.batch) &&
+      tma_legal(p.in, in->pitch, in->batch_stride, p.batch)) {
+    AdjFusedParams P;
+    memset(&P, 0, sizeof(P));
+    const int fh = AF_TH + 2 * (K / 2);
+    if (make_tensor_map_3d(&P.map_g, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p.gout, p.w, p.h, p.batch, grad_out->pitch,
+                           grad_out->batch_stride, AF_W, fh) == HGB_OK &&
+        make_tensor_map_3d(&P.map_x, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p.in, p.w, p.h, p.batch, in->pitch,
+                           in->batch_stride, AF_W, fh) == HGB_OK) {
+      P.p = p;
+      P.status = device_status_word();
+      P.tiles_x = cdiv(p.w, AF_TW);
+      P.tiles_y = cdiv(p.h, AF_TH);
+      P.ntiles = P.tiles_x * P.tiles_y * p.batch;
+      P.vec_gin = ((uintptr_t)grad_in->data % 16 == 0 && grad_in->pitch % 16 == 0 &&
+                   (p.batch == 1 || grad_in->batch_stride % 16 == 0))
+                      ? 1
+                      : 0;
+      const void *kern = K == 3 ? (const void *)adj_fused_kernel<3>
+                                : (K == 5 ? (const void *)adj_fused_kernel<5> : (const void *)adj_fused_kernel<7>);
+      const int grid = std::max(1, std::min(P.ntiles, num_sms() * resident_ctas(kern, LA_T, 0)));
+      Workspace ws;
+      rc = workspace_get((size_t)K * K * grid * 4 + 64, &ws);
+      if (rc) return rc;
+      P.p.part = (float *)ws.base;
+      cudaEvent_t ev = before_launch(st);
+      if (K == 3)
+        adj_fused_kernel<3><<<grid, LA_T, 0, st>>>(P);
+      else if (K == 5)
+        adj_fused_kernel<5><<<grid, LA_T, 0, st>>>(P);
+      else
+        adj_fused_kernel<7><<<grid, LA_T, 0, st>>>(P);
+      adj_mask_combine<<<K * K, LA_T, 0, st>>>(P.p, grid);
+      return after_launch("local_op_adjoint fused", st, ev);
+    }
+  }
   cudaEvent_t ev = before_launch(st);
   if (grad_in) {
     const dim3 tg(cdiv(p.w, LM_TW), cdiv(p.h, LM_TH), p.batch);
