@@ -410,7 +410,8 @@ def gauss_taps(k, sigma):
     return (g / g.sum()).astype(np.float32)
 
 
-OTHER_SECTIONS = ("integer", "gaussian", "precision", "pyramid", "diff", "histogram", "pipelines", "extras")
+OTHER_SECTIONS = ("integer", "gaussian", "precision", "pyramid", "diff", "histogram", "pipelines", "extras",
+                  "pyramid_trace")
 
 
 def measure_other_configs(dev, peak_gbs, only=None):
@@ -429,6 +430,8 @@ def measure_other_configs(dev, peak_gbs, only=None):
 
     if only == "integer":  # the headline step's two kernels alone, few launches (for a profiler)
         _integer(dev, peak_gbs, s, res)
+    if only == "pyramid_trace":  # where the single launch spends its time (measurement only)
+        _pyramid_trace(dev, s, res)
     if want("gaussian"):
         _gaussian(dev, peak_gbs, s, res, q)
     if want("precision"):
@@ -678,12 +681,12 @@ def _precision_errors(img, taps, sm):
     return out
 
 
-def _pyramid(dev, peak_gbs, s, res, q):
+def _pyramid_batch(dev):
+    """The pyramid workload: 64 FP32 images, w and h uniform in [257, 4096], 8 levels, MIRROR."""
     import torch
 
     from hipacc_gb300 import api
 
-    # batching: 64 FP32 images, w and h uniform in [257, 4096], 8-level Laplacian pyramid, MIRROR
     rng = np.random.default_rng(4096)
     ws_ = rng.integers(257, 4097, 64)
     hs_ = rng.integers(257, 4097, 64)
@@ -692,6 +695,75 @@ def _pyramid(dev, peak_gbs, s, res, q):
     plan = api.PyramidPlan(ws_, hs_, levels, np.outer(b1, b1).astype(np.float32), api.MIRROR)
     for i in range(64):
         plan.gauss(i, 0).copy_(torch.rand((int(hs_[i]), int(ws_[i])), device=dev))
+    return plan, ws_, hs_, levels, b1
+
+
+def _pyramid_trace(dev, s, res):
+    """Per-CTA records of the three single-launch forms (hgb_pyramid_plan_trace), each at the tile
+    configuration the autotuner picks for the single launch, beside the per-level launches: where
+    the time goes (tile claims, waits on the previous level, tiles, the tail of the launch)."""
+    import tempfile
+
+    import torch
+
+    from hipacc_gb300 import api
+
+    plan, ws_, hs_, levels, b1 = _pyramid_batch(dev)
+    api.autotune(True)
+    plan.decompose(0, stream=s)
+    plan.decompose(1, stream=s)
+    s.synchronize()
+    api.autotune(False)
+    tuned = os.path.join(tempfile.gettempdir(), f"hgb_pyr_trace_{os.getpid()}.json")
+    api.L.call("hgb_autotune_save", tuned.encode())
+    table = json.load(open(tuned))
+    key = [k for k in table if k.startswith("pyramid:m0:")][0]
+    cfg = int(table[key][0]) % 4
+    res["pyramid_trace_config"] = {"key": key, "autotuned": table[key], "tile_config": cfg}
+    res["per_level_7launches_us"] = graph_time_us(lambda i: plan.decompose(1, stream=s), 1, s, 5)
+    cap = 400000
+    buf = torch.zeros(8 * cap, dtype=torch.int64, device=dev)
+    for single, name in ((0, "persistent_claims"), (1, "one_cta_per_tile"), (2, "cooperative_static_level0")):
+        json.dump({key: [single * 4 + cfg, 0.0]}, open(tuned, "w"))
+        api.L.call("hgb_autotune_load", tuned.encode())
+        us = graph_time_us(lambda i: plan.decompose(0, stream=s), 1, s, 5)
+        buf.zero_()
+        plan.trace(buf)
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(s)
+        plan.decompose(0, stream=s)
+        stop.record(s)
+        s.synchronize()
+        plan.trace(None)
+        r = buf.view(-1, 8).cpu().numpy()
+        r = r[r[:, 1] > 0]
+        t0, t1, c0, c1 = r[:, 0], r[:, 1], r[:, 2], r[:, 3]
+        life = (c1 - c0).astype(np.float64)
+        span = float(t1.max() - t0.min())
+        ends = np.sort(t1 - t0.min()) / 1e3
+        tiles = (r[:, 7] & 0xffffffff).astype(np.int64)
+        polled = (r[:, 7] >> 32).astype(np.int64)
+        res[f"pyramid_trace_{name}"] = {
+            "us_untraced": us, "us_traced": start.elapsed_time(stop) * 1e3, "ctas": int(len(r)),
+            "span_us": span / 1e3, "tiles": int(tiles.sum()), "waits_that_polled": int(polled.sum()),
+            "share_of_cta_cycles": {"claim": float(r[:, 4].sum() / life.sum()),
+                                    "level_wait": float(r[:, 5].sum() / life.sum()),
+                                    "tiles": float(r[:, 6].sum() / life.sum())},
+            "cta_end_us_quantiles": {"first": float(ends[0]), "p10": float(np.quantile(ends, 0.1)),
+                                     "p50": float(np.quantile(ends, 0.5)), "p90": float(np.quantile(ends, 0.9)),
+                                     "last": float(ends[-1])},
+        }
+    os.remove(tuned)
+    plan.close()
+
+
+def _pyramid(dev, peak_gbs, s, res, q):
+    import torch
+
+    from hipacc_gb300 import api
+
+    # batching: 64 FP32 images, w and h uniform in [257, 4096], 8-level Laplacian pyramid, MIRROR
+    plan, ws_, hs_, levels, b1 = _pyramid_batch(dev)
     base_px = float(np.sum(ws_.astype(np.int64) * hs_))
     alg = 0.0
     for i in range(64):

@@ -91,6 +91,7 @@ SIGNATURES = {
     "hgb_pyramid_decompose": (i32, [vp, i32, vp]),
     "hgb_pyramid_collapse": (i32, [vp, vp]),
     "hgb_pyramid_plan_wait_test": (i32, [vp, C.c_longlong, i32, i32]),
+    "hgb_pyramid_plan_trace": (i32, [vp, vp, C.c_longlong]),
     "hgb_local_op_adjoint": (i32, [VP, VP, VP, vp, vp, i32, i32, i32, vp, vp]),
     "hgb_bilateral_adjoint": (i32, [VP, VP, vp, i32, f32, i32, f32, VP, vp, vp]),
     "hgb_conv_bilateral_mse": (i32, [VP, VP, vp, i32, vp, i32, vp, i32, i32, vp, VP, vp, vp, vp]),

@@ -248,6 +248,14 @@ class PyramidPlan:
         """Bounded-wait test mode of the plan's launches (hgb_pyramid_plan_wait_test)."""
         L.call("hgb_pyramid_plan_wait_test", self._h, int(max_polls), int(kind), int(level))
 
+    def trace(self, buf=None):
+        """Per-CTA records of later single-launch decompositions into `buf` (an
+        int64 CUDA tensor of 8 * CTAs), or off with None (hgb_pyramid_plan_trace)."""
+        if buf is None:
+            L.call("hgb_pyramid_plan_trace", self._h, None, 0)
+        else:
+            L.call("hgb_pyramid_plan_trace", self._h, C.c_void_p(buf.data_ptr()), buf.numel() // 8)
+
     def collapse(self, stream=None):
         L.call("hgb_pyramid_collapse", self._h, _stream(stream))
 

@@ -104,7 +104,23 @@ struct PyrParams {
   int inject_level;
   float mask[25];
   int bmode;
+  long long *trace;         // persistent form, when set: one PyrTrace record per CTA
 };
+
+// Per-CTA trace of the single-launch forms (thread 0's view): start and end
+// (global timer, ns, and the SM clock), SM clock cycles spent in tile claims,
+// in level waits and in tiles (work, barrier and publish), tiles taken, and
+// waits that had to poll.
+struct PyrTrace {
+  long long t0, t1, c0, c1, claim, wait, tile, counts;  // counts: tiles | polled waits << 32
+};
+static_assert(sizeof(PyrTrace) == 8 * sizeof(long long), "trace record");
+
+__device__ __forceinline__ long long global_ns() {
+  long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ float ld_level(const float *p, bool coherent) {
   // levels written inside the same persistent launch must bypass the
@@ -381,7 +397,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_level_kernel(const __g
 // claiming one tile when the hardware starts it.  Either way a tile only waits
 // on tiles claimed before it, so the claimers of what it waits for are running
 // or done.
-template <class C>
+template <class C, bool TRACE>
 __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(const __grid_constant__ PyrParams p) {
   __shared__ __align__(128) float stage[C::BW * C::BH];
   __shared__ float gt[C::GW * C::GH];
@@ -403,6 +419,21 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(cons
   // whole launch); tiles are processed in list order.
   int claim_base = 0, claim_left = 0;
   int static_next = p.single == 2 ? (int)blockIdx.x : p.nlevel0;
+  // the trace record lives in shared memory (thread 0 only), so that it costs
+  // the tile loop no registers
+  __shared__ PyrTrace tr;
+  if (TRACE && threadIdx.x == 0) {
+    tr = PyrTrace{};
+    tr.t0 = global_ns();
+    tr.c0 = clock64();
+  }
+  auto trace_out = [&]() {
+    if (TRACE && threadIdx.x == 0) {
+      tr.t1 = global_ns();
+      tr.c1 = clock64();
+      reinterpret_cast<PyrTrace *>(p.trace)[blockIdx.x] = tr;
+    }
+  };
   for (;;) {
     if (threadIdx.x == 0) {
       int t;
@@ -412,7 +443,9 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(cons
       } else {
         if (claim_left == 0) {
           const int chunk = p.single == 1 ? 1 : kPyClaim;
+          if (TRACE) tr.c1 = clock64();
           claim_base = (int)atomicAdd(p.work, (unsigned)chunk) + (p.single == 2 ? p.nlevel0 : 0);
+          if (TRACE) tr.claim += clock64() - tr.c1;
           claim_left = chunk;
         }
         t = claim_base++;
@@ -428,6 +461,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(cons
           const int k = tl.img * p.levels + tl.level - 1;
           const unsigned int need = (unsigned int)p.ntiles_il[k];
           long long spins = 0;
+          if (TRACE) tr.c1 = clock64();
           while (ld_acquire_u32(&p.done[k]) < need) {
             if (ld_acquire_u32(p.abort)) {
               s_ok = 0;
@@ -441,6 +475,10 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(cons
             }
             __nanosleep(64);
           }
+          if (TRACE) {
+            tr.wait += clock64() - tr.c1;
+            if (spins) tr.counts += 1ll << 32;
+          }
         }
         // wait test kind 1: the tile is claimed but never published
         if (s_ok == 1 && tl.level == p.inject_level && p.inject_kind == 1) s_ok = 2;
@@ -448,8 +486,12 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(cons
     }
     __syncthreads();
     const int t = s_t;
-    if (t >= p.ntiles || s_ok == 0) return;
+    if (t >= p.ntiles || s_ok == 0) {
+      trace_out();
+      return;
+    }
     const PyrTile tl = p.tiles[t];
+    if (TRACE && threadIdx.x == 0) tr.c1 = clock64();  // tile start (c1 is final only at exit)
     if (s_ok == 2) {  // uniform: every thread read s_ok after the barrier
       if (p.single == 1) return;
       __syncthreads();  // s_t / s_ok are read before thread 0 claims again
@@ -461,7 +503,14 @@ __global__ void __launch_bounds__(C::NT, C::MIN_CTAS) pyr_persistent_kernel(cons
     }
     __syncthreads();
     if (threadIdx.x == 0) red_release_add(&p.done[tl.img * p.levels + tl.level], 1u);
-    if (p.single == 1) return;
+    if (TRACE && threadIdx.x == 0) {
+      tr.tile += clock64() - tr.c1;
+      tr.counts += 1;
+    }
+    if (p.single == 1) {
+      trace_out();
+      return;
+    }
   }
 }
 
@@ -540,6 +589,8 @@ struct hgb_pyramid_plan {
   PyrConfigData cfg[kPyCfgs];
   long long max_polls = kMaxSpins;
   int inject_kind = 0, inject_level = 0;
+  long long *trace = nullptr;  // device buffer of PyrTrace records (hgb_pyramid_plan_trace)
+  long long trace_cap = 0;     // records it holds
 };
 
 namespace {
@@ -572,6 +623,11 @@ int build_config(hgb_pyramid_plan *P, int c) {
     D.level_count.push_back((int)tiles.size() - D.level_first.back());
   }
   D.ntiles = (int)tiles.size();
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pyr_persistent_kernel<C, false>, C::NT, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  D.persistent_ctas = num_sms() * per_sm;
   // tensor maps of every Gaussian level a tile stages
   std::vector<CUtensorMap> maps(P->meta.size());
   memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
@@ -591,11 +647,6 @@ int build_config(hgb_pyramid_plan *P, int c) {
   if (e == cudaSuccess)
     e = cudaMemcpy(D.d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_error(e, "hgb_pyramid_plan_create: work-list upload");
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pyr_persistent_kernel<C>, C::NT, 0) != cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
-  D.persistent_ctas = num_sms() * per_sm;
   return HGB_OK;
 }
 
@@ -742,15 +793,20 @@ static int launch_decompose(const hgb_pyramid_plan *P, int c, int mode, int sing
     p.single = single;
     p.nlevel0 = D.level_count[0];
     const int grid = single == 1 ? D.ntiles : std::min(D.persistent_ctas, D.ntiles);
+    p.trace = (P->trace && grid <= P->trace_cap) ? P->trace : nullptr;
     cudaEvent_t ev = before_launch(st);
+    // the traced instantiation only when a trace buffer is set (measurement)
+    const void *kern =
+        p.trace ? (const void *)pyr_persistent_kernel<C, true> : (const void *)pyr_persistent_kernel<C, false>;
     if (single == 2) {
       // co-residency of the whole grid is what makes the static level-0 share
       // safe: a cooperative launch fails instead of running a partial grid
       void *args[] = {(void *)&p};
-      HGB_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)pyr_persistent_kernel<C>, dim3(grid), dim3(C::NT),
-                                                 args, 0, st));
+      HGB_CHECK_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(C::NT), args, 0, st));
+    } else if (p.trace) {
+      pyr_persistent_kernel<C, true><<<grid, C::NT, 0, st>>>(p);
     } else {
-      pyr_persistent_kernel<C><<<grid, C::NT, 0, st>>>(p);
+      pyr_persistent_kernel<C, false><<<grid, C::NT, 0, st>>>(p);
     }
     return after_launch("pyr_persistent_kernel", st, ev);
   }
@@ -813,6 +869,14 @@ int hgb_pyramid_decompose(hgb_pyramid_plan *P, int mode, void *stream) {
       if (rc) return rc;
     }
   }
+  return HGB_OK;
+}
+
+int hgb_pyramid_plan_trace(hgb_pyramid_plan *P, long long *trace_dev, long long capacity) {
+  HGB_REQUIRE(P, "hgb_pyramid_plan_trace: null plan");
+  HGB_REQUIRE(capacity >= 0 && (trace_dev != nullptr || capacity == 0), "hgb_pyramid_plan_trace: bad buffer");
+  P->trace = trace_dev;
+  P->trace_cap = capacity;
   return HGB_OK;
 }
 

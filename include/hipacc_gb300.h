@@ -351,6 +351,14 @@ HGB_API int hgb_pyramid_collapse(hgb_pyramid_plan *plan, void *stream);
  * HGB_ERR_TIMEOUT (hgb_device_status) and the context stays usable; nothing
  * faults or traps. */
 HGB_API int hgb_pyramid_plan_wait_test(hgb_pyramid_plan *plan, long long max_polls, int kind, int level);
+/* Measurement support for the single-launch form (no counterpart in the
+ * reference): when `trace_dev` is set, each CTA of a later mode-0 launch whose
+ * grid has at most `capacity` CTAs writes one record of 8 int64 at
+ * trace_dev[8 * cta]: start and end on the global timer (ns) and on the SM
+ * clock, SM clock cycles spent claiming tiles, waiting for previous levels and
+ * running tiles, then (tiles taken) | (waits that polled) << 32.  NULL turns
+ * it off. */
+HGB_API int hgb_pyramid_plan_trace(hgb_pyramid_plan *plan, long long *trace_dev, long long capacity);
 
 /* ------------------------------------------------------------------ */
 /* adjoints                                                            */

@@ -279,3 +279,48 @@ def test_pyramid_single_launch_in_a_graph(gpu, oracle, k, tmp_path):
     finally:
         L.call("hgb_autotune_clear")
         plan.close()
+
+
+def test_pyramid_trace_records(gpu, oracle, tmp_path):
+    """The single launch's per-CTA trace (hgb_pyramid_plan_trace) in each form:
+    the traced launch is still bit-exact, every tile is counted once, and every
+    record is well formed (end after start, parts within the CTA's lifetime)."""
+    import json
+    import math
+
+    from hipacc_gb300 import _lib as L
+
+    levels = 6
+    plan, imgs = _plan(gpu, oracle, SIZES, levels, oracle.MIRROR, 13)
+    px = sum(w * h for (w, h) in SIZES)
+    key = "pyramid:m0:n%d:l%d:px2^%d" % (len(SIZES), levels, math.ceil(math.log2(px)))
+    refs = [oracle.pyramid_decompose(im, levels, oracle.binomial5(), oracle.MIRROR, contract=1) for im in imgs]
+    buf = torch.zeros(8 * 20000, dtype=torch.int64, device="cuda")
+    counts = []
+    for single in (0, 1, 2):
+        f = tmp_path / "choice.json"
+        f.write_text(json.dumps({key: [single * 4, 0.0]}))
+        L.call("hgb_autotune_clear")
+        L.call("hgb_autotune_load", str(f).encode())
+        buf.zero_()
+        plan.trace(buf)
+        plan.decompose(0)
+        torch.cuda.synchronize()
+        plan.trace(None)
+        r = buf.view(-1, 8).cpu().numpy()
+        r = r[r[:, 1] > 0]
+        assert len(r) > 0
+        assert np.all(r[:, 1] >= r[:, 0]) and np.all(r[:, 3] >= r[:, 2])
+        life = r[:, 3] - r[:, 2]
+        assert np.all(r[:, 4] + r[:, 5] + r[:, 6] <= life)
+        ntiles = int((r[:, 7] & 0xffffffff).sum())
+        counts.append(ntiles)
+        for i, (g, lap) in enumerate(refs):
+            for l in range(levels):
+                assert np.array_equal(plan.gauss(i, l).cpu().numpy(), g[l]), (single, i, l)
+                if l + 1 < levels:
+                    assert np.array_equal(plan.lap(i, l).cpu().numpy(), lap[l]), (single, i, l)
+    # the same work-list in every form: each tile taken exactly once
+    assert counts[0] > 0 and counts[0] == counts[1] == counts[2], counts
+    L.call("hgb_autotune_clear")
+    plan.close()
