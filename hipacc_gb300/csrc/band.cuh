@@ -3,7 +3,8 @@
 // A tile path that takes groups of four horizontally adjacent pixels whose
 // taps stay inside the image leaves out a band of radius R along the edges:
 // rows [0, R) and [H-R, H) whole, then, for the rows in between, columns
-// [0, 4) and [W-wr, W) with wr = W - 4 floor((W - R) / 4).  Those pixels go
+// [0, L) and [W-wr, W) with L = R rounded up to 4 and wr = W - 4 floor((W -
+// R) / 4) (the image must be wide enough that the two do not meet).  Those pixels go
 // through the boundary's pre-images one pixel per thread, from a flat list of
 // the batch's band pixels that every CTA takes an equal contiguous share of.
 #pragma once
@@ -12,9 +13,10 @@
 
 namespace hgb {
 
+__host__ __device__ __forceinline__ int band_left(int R) { return (R + 3) / 4 * 4; }
 __host__ __device__ __forceinline__ int band_right(int W, int R) { return W - 4 * ((W - R) / 4); }
 __host__ __device__ __forceinline__ int band_size(int W, int H, int R) {
-  return 2 * R * W + (H - 2 * R) * (4 + band_right(W, R));
+  return 2 * R * W + (H - 2 * R) * (band_left(R) + band_right(W, R));
 }
 __device__ __forceinline__ void band_pos(int k, int W, int H, int R, int &y, int &x) {
   if (k < 2 * R * W) {
@@ -24,10 +26,10 @@ __device__ __forceinline__ void band_pos(int k, int W, int H, int R, int &y, int
     return;
   }
   k -= 2 * R * W;
-  const int mid = (H - 2 * R) * 4;
+  const int L = band_left(R), mid = (H - 2 * R) * L;
   if (k < mid) {
-    y = R + (k >> 2);
-    x = k & 3;
+    y = R + k / L;
+    x = k - (y - R) * L;
     return;
   }
   k -= mid;

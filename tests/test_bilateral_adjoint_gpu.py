@@ -48,6 +48,28 @@ def test_bilateral_adjoint_vs_fp64_oracle(gpu, oracle, boundary, const, size, hw
     assert abs(gs - ref_gs) <= max(ADJ_TOL * abs(ref_gs), SIGMA_ABS), (gs, ref_gs)
 
 
+@pytest.mark.parametrize("boundary,const", [(1, 0.0), (2, 0.0), (3, 0.0), (4, 0.5)])
+@pytest.mark.parametrize("size", [3, 7, 11])
+def test_bilateral_adjoint_many_tiles(gpu, oracle, boundary, const, size):
+    """Symmetric masks on images of several 64 x 16 tiles with ragged edges
+    (the packed form: tiles, then the edge band by pre-images): every pixel
+    of dL/din against the FP64 oracle, and dL/dsigma_r."""
+    rng = np.random.default_rng(size * 100 + boundary)
+    B, h, w = 2, 53, 203
+    x = rng.random((B, h, w), dtype=np.float32)
+    g = rng.normal(0, 1, (B, h, w)).astype(np.float32)
+    sm = oracle.spatial_mask(size, size / 4.0)
+    sigma = 0.2
+    gi, gs = _gpu(gpu, x, g, sm, sigma, boundary, const)
+    ref_gs = 0.0
+    for b in range(B):
+        a, sg = oracle.bilateral_adjoint(x[b], g[b], sm.astype(np.float64), sigma, boundary, const)
+        ref_gs += sg
+        err = np.abs(gi[b] - a)
+        assert np.max(err) <= 2e-3 * np.max(np.abs(a)), (b, np.unravel_index(np.argmax(err), err.shape))
+    assert abs(gs - ref_gs) <= max(ADJ_TOL * abs(ref_gs), SIGMA_ABS), (gs, ref_gs)
+
+
 @pytest.mark.parametrize("boundary", [1, 3])
 def test_bilateral_adjoint_vs_central_differences(gpu, oracle, boundary):
     """L = sum(g * bilateral(x)) in FP64; central differences with eps = 1e-4
