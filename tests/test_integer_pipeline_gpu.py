@@ -63,31 +63,45 @@ def test_sobel_pitched_tma_path(gpu, oracle, b, hw):
 @pytest.mark.parametrize("cfg", [0, 1])
 def test_sobel_every_tile_configuration(gpu, oracle, cfg, tmp_path):
     """Each configuration the autotuner can choose for the staged Sobel (rows
-    per warp), forced through a loaded choice file, is bit-exact."""
+    per warp), forced through a loaded choice file, is bit-exact: ragged
+    tiles, warps whose rows lie below the image, every boundary mode,
+    low-contrast images whose maximum is below 255, a batch."""
     import json
 
     from hipacc_gb300 import _lib as L
 
     rng = np.random.default_rng(40 + cfg)
-    for (h, w) in [(777, 1001), (512, 512), (4096, 4096)]:
-        img = rng.integers(0, 256, (h, w), dtype=np.uint8)
+    cases = [((777, 1001), 3, 256, 1), ((512, 512), 3, 256, 1), ((4096, 4096), 3, 256, 1),
+             ((100, 300), 1, 256, 1), ((33, 129), 2, 256, 1), ((1, 64), 4, 256, 1), ((130, 17), 3, 256, 1),
+             ((300, 700), 3, 9, 1), ((257, 390), 4, 256, 3), ((96, 160), 2, 5, 2)]
+    for (h, w), bnd, hi, nb in cases:
+        imgs = rng.integers(0, hi, (nb, h, w), dtype=np.uint8)
         wp = (w + 15) // 16 * 16
-        dev = torch.zeros((h, wp), dtype=torch.uint8, device="cuda")
-        dev[:, :w] = torch.from_numpy(img).cuda()
-        out = torch.zeros((h, wp), dtype=torch.uint8, device="cuda")
-        key = "sobel3:%dx%dx1" % (1 << w.bit_length(), 1 << h.bit_length())
+        dev = torch.zeros((nb, h, wp), dtype=torch.uint8, device="cuda")
+        dev[:, :, :w] = torch.from_numpy(imgs).cuda()
+        out = torch.zeros((nb, h, wp), dtype=torch.uint8, device="cuda")
+        key = "sobel3:%dx%dx%d" % (1 << w.bit_length(), 1 << h.bit_length(), nb)
         f = tmp_path / "choice.json"
         f.write_text(json.dumps({key: [cfg, 0.0]}))
         L.call("hgb_autotune_clear")
         L.call("hgb_autotune_load", str(f).encode())
         s = torch.zeros(1, dtype=torch.int64, device="cuda")
         m = torch.zeros(1, dtype=torch.int32, device="cuda")
-        gpu.sobel_mag(dev[:, :w], out[:, :w], boundary=3, sum_out=s, max_out=m)
+        src, dst = (dev[:, :, :w], out[:, :, :w]) if nb > 1 else (dev[0, :, :w], out[0, :, :w])
+        gpu.sobel_mag(src, dst, boundary=bnd, const=17, sum_out=s, max_out=m)
         torch.cuda.synchronize()
         L.call("hgb_autotune_clear")
-        ref = oracle.sobel_mag(img, boundary=3)
-        assert np.array_equal(out[:, :w].cpu().numpy(), ref), (h, w)
-        assert s.item() == int(ref.astype(np.uint64).sum()) and m.item() == int(ref.max())
+        refs = [oracle.sobel_mag(imgs[i], boundary=bnd, const=17) for i in range(nb)]
+        got = out.cpu().numpy()
+        for i, ref in enumerate(refs):
+            assert np.array_equal(got[i, :, :w], ref), (h, w, bnd, i)
+        assert s.item() == sum(int(r.astype(np.uint64).sum()) for r in refs), (h, w)
+        assert m.item() == max(int(r.max()) for r in refs), (h, w)
+    import ctypes as C
+
+    status = C.c_int(-1)
+    L.call("hgb_device_status", C.byref(status))
+    assert status.value == L.OK
 
 
 def test_sobel_4096_mirror(gpu, oracle):
