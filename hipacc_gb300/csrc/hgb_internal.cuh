@@ -48,6 +48,7 @@ constexpr int kAcc = 64;
 // accumulator / ticket slots of the fused and standalone reductions
 constexpr int kSlotSobel = 0;   // acc[0] sum, acc[1] max; ticket[0]
 constexpr int kSlotReduce = 2;  // acc[2]; ticket[1]
+constexpr int kTicketSobelClaim = 3;  // tile counter of the streaming Sobel
 int workspace_get(size_t bytes, Workspace *ws);  // grows on demand
 
 int num_sms();

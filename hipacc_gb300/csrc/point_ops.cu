@@ -354,12 +354,14 @@ __global__ void __launch_bounds__(256) resample_kernel(const char *in, int64_t i
 // Dense images (rows back to back, the batch contiguous) are one flat array of
 // N pixels, cut into units of GB_UNIT pixels (16 KiB of uchar4).  Each CTA
 // takes one unit: thread 0 issues one cp.async.bulk of the unit into shared
-// memory (completion on an mbarrier) and every thread turns four groups of
-// four staged pixels, 4 KiB apart, into four 4-byte stores.  With 16 KiB of shared memory per CTA the SM holds
-// up to 8 such CTAs, so many copies are in flight without a software pipeline,
-// and an independent kernel of the same step can share the SMs.  The last CTA
-// converts the pixels after the last whole unit with plain loads.
-constexpr int GB_T = 256, GB_UNIT = 16 * GB_T;
+// memory (completion on an mbarrier) and every thread turns GB_PX / 4 groups
+// of four staged pixels, GB_T groups apart, into 4-byte stores.  With 16 KiB
+// of shared memory per CTA the SM holds many such CTAs, so many copies are in
+// flight without a software pipeline, and an independent kernel of the same
+// step can share the SMs.  The last CTA converts the pixels after the last
+// whole unit with plain loads.
+constexpr int GB_T = 256, GB_PX = 16;
+constexpr int GB_UNIT = GB_PX * GB_T;
 constexpr int GB_STAGE = GB_UNIT * 4;
 
 struct GrayBulkParams {
@@ -399,7 +401,7 @@ __global__ void __launch_bounds__(GB_T) gray_bulk_kernel(const __grid_constant__
     const uint4 *src = reinterpret_cast<const uint4 *>(stage) + threadIdx.x;
     uint32_t *dst = reinterpret_cast<uint32_t *>(p.out + u * GB_UNIT) + threadIdx.x;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < GB_PX / 4; ++k) {
       const uint4 q = src[k * GB_T];
       dst[k * GB_T] = gray_px(p, q.x) | (gray_px(p, q.y) << 8) | (gray_px(p, q.z) << 16) | (gray_px(p, q.w) << 24);
     }

@@ -233,14 +233,23 @@ struct SobelTmaParams {
   int *status;
   unsigned long long *acc;  // workspace accumulators (sum, max), zero at rest
   unsigned int *ticket;
+  unsigned int *claim;      // tile counter of the streaming form, zero at rest
 };
 
-// the tile is 128 x 128 outputs in either configuration; the autotuner picks
-// the rows per warp: 32 rows for 4 warps, or 16 rows for 8 warps (a shorter
-// serial stencil per warp after the tile lands, twice the warps per SM)
+// The tile is 128 x 128 outputs in every configuration.  The autotuner picks
+// the rows per warp (32 rows for 4 warps, or 16 rows for 8 warps: a shorter
+// serial stencil per warp after the tile lands, twice the warps per SM) and the
+// launch form:
+//   one-shot (kSobelStream 0): one CTA per tile, every tile's copy issued at
+//     launch;
+//   streaming (kSobelStream = CTAs per SM): a few CTAs per SM claim tiles from
+//     a counter, each with two stage buffers, so that the next tile's copy
+//     lands while the current one is computed.  Tiles go to the CTAs that are
+//     free, and the SMs keep room for an independent kernel of the same step.
 constexpr int T_TW = 128, T_TH = 128;
-constexpr int kSobelWarps[] = {4, 8};
-constexpr int kSobelCfgs = 2;
+constexpr int kSobelWarps[] = {4, 8, 4, 4, 8};
+constexpr int kSobelStream[] = {0, 0, 2, 3, 2};
+constexpr int kSobelCfgs = 5;
 constexpr int T_SW = 160, T_SH = T_TH + 2, T_STAGE = T_SW * T_SH;
 constexpr int T_STAGE_PAD = (T_STAGE + 127) / 128 * 128;
 
@@ -323,6 +332,40 @@ __device__ __forceinline__ void sobel_tile(const SobelParams &p, const uint8_t *
   }
 }
 
+// Staged cells outside the image that the stencil reads (columns 15..144, all
+// rows of a tile whose first staged cell is image (X0, Y0)) get the boundary
+// rule; TMA filled them with zeros.  Regions: left columns, right columns, top
+// row, bottom rows.  Every thread of the CTA takes part.
+__device__ __forceinline__ void sobel_patch(const SobelParams &p, const uint8_t *img, uint8_t *tile, int X0, int Y0) {
+  constexpr int qa = 15, qb = 145, ncol = qb - qa;
+  const int nl = max(0, min(qb, -X0) - qa);
+  const int rs = max(qa, p.w - X0), nr = max(0, qb - rs);
+  const int ntop = max(0, -Y0);
+  const int bs = max(0, p.h - Y0), nb = max(0, T_SH - bs);
+  const int n1 = nl * T_SH, n2 = n1 + nr * T_SH, n3 = n2 + ntop * ncol, n4 = n3 + nb * ncol;
+  for (int cc = threadIdx.x; cc < n4; cc += blockDim.x) {
+    int r, q;
+    if (cc < n1) {
+      r = cc / nl;
+      q = qa + (cc - r * nl);
+    } else if (cc < n2) {
+      const int d = cc - n1;
+      r = d / nr;
+      q = rs + (d - r * nr);
+    } else if (cc < n3) {
+      const int d = cc - n2;
+      r = d / ncol;
+      q = qa + (d - r * ncol);
+    } else {
+      const int d = cc - n3;
+      const int rr = d / ncol;
+      r = bs + rr;
+      q = qa + (d - rr * ncol);
+    }
+    tile[r * T_SW + q] = (uint8_t)sb_load_px(p, img, X0 + q, Y0 + r);
+  }
+}
+
 template <int T_WARPS>
 __global__ void __launch_bounds__(T_WARPS * 32) sobel3_tma_kernel(const __grid_constant__ SobelTmaParams P) {
   constexpr int T_R = T_TH / T_WARPS;
@@ -352,37 +395,7 @@ __global__ void __launch_bounds__(T_WARPS * 32) sobel3_tma_kernel(const __grid_c
   }
   const int X0 = i0 - 16, Y0 = j0 - 1;
   if (X0 + 15 < 0 || X0 + 145 > p.w || Y0 < 0 || Y0 + T_SH > p.h) {
-    // Patch the staged cells outside the image that the stencil reads
-    // (columns 15..144, all rows) with the boundary rule; TMA filled them
-    // with zeros.  Regions: left columns, right columns, top row, bottom rows.
-    const uint8_t *img = p.in + (int64_t)b * p.in_bstride;
-    constexpr int qa = 15, qb = 145, ncol = qb - qa;
-    const int nl = max(0, min(qb, -X0) - qa);
-    const int rs = max(qa, p.w - X0), nr = max(0, qb - rs);
-    const int ntop = max(0, -Y0);
-    const int bs = max(0, p.h - Y0), nb = max(0, T_SH - bs);
-    const int n1 = nl * T_SH, n2 = n1 + nr * T_SH, n3 = n2 + ntop * ncol, n4 = n3 + nb * ncol;
-    for (int cc = threadIdx.x; cc < n4; cc += T_WARPS * 32) {
-      int r, q;
-      if (cc < n1) {
-        r = cc / nl;
-        q = qa + (cc - r * nl);
-      } else if (cc < n2) {
-        const int d = cc - n1;
-        r = d / nr;
-        q = rs + (d - r * nr);
-      } else if (cc < n3) {
-        const int d = cc - n2;
-        r = d / ncol;
-        q = qa + (d - r * ncol);
-      } else {
-        const int d = cc - n3;
-        const int rr = d / ncol;
-        r = bs + rr;
-        q = qa + (d - rr * ncol);
-      }
-      tile[r * T_SW + q] = (uint8_t)sb_load_px(p, img, X0 + q, Y0 + r);
-    }
+    sobel_patch(p, p.in + (int64_t)b * p.in_bstride, tile, X0, Y0);
     __syncthreads();
   }
   uint32_t tsum = 0;
@@ -413,6 +426,113 @@ __global__ void __launch_bounds__(T_WARPS * 32) sobel3_tma_kernel(const __grid_c
         M = M > s_max[i] ? M : s_max[i];
       }
       accumulate_and_publish(P.acc, P.acc + 1, P.ticket, S, M, p.sum_dev, p.max_dev);
+    }
+  }
+}
+
+// Streaming form: gridDim.x CTAs (a few per SM) claim tiles from P.claim.
+// Thread 0 keeps two tiles' copies in flight, one per stage buffer; after a
+// tile is computed and every thread's reads of its buffer are done (CTA
+// barrier, then a proxy fence), the buffer takes the next claimed tile.  The
+// tile numbers travel through shared memory: slot k & 1 is rewritten only
+// after the barrier that follows its use, and read only after the barrier
+// that follows its rewrite.  Every CTA ends by taking one ticket; the last one
+// publishes the sum and maximum and returns the counters to zero.
+template <int T_WARPS>
+__global__ void __launch_bounds__(T_WARPS * 32) sobel3_stream_kernel(const __grid_constant__ SobelTmaParams P) {
+  constexpr int T_R = T_TH / T_WARPS;
+  __shared__ __align__(128) uint8_t tile[2][T_STAGE_PAD];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ int s_tile[2];
+  __shared__ unsigned long long s_sum[T_WARPS];
+  __shared__ uint32_t s_max[T_WARPS];
+  const SobelParams &p = P.p;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto issue = [&](int k, int t) {  // thread 0: tile t into buffer k
+    const int tx_ = t % P.tiles_x, r_ = t / P.tiles_x;
+    mbar_expect_tx(&bar[k], T_STAGE);
+    tma_load_3d(tile[k], &P.map, tx_ * T_TW - 16, (r_ % P.tiles_y) * T_TH - 1, r_ / P.tiles_y, &bar[k]);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+    for (int k = 0; k < 2; ++k) {
+      const int t = (int)atomicAdd(P.claim, 1u);
+      s_tile[k] = t;
+      if (t < P.ntiles) issue(k, t);
+    }
+  }
+  __syncthreads();
+  unsigned long long tsum64 = 0;
+  __half2 tmax = __float2half2_rn(0.0f);
+  for (int k = 0;; ++k) {
+    const int buf = k & 1;
+    const int t = s_tile[buf];
+    if (t >= P.ntiles) break;  // the same value in every thread: the CTA leaves together
+    if (!cta_wait(&bar[buf], (k >> 1) & 1)) {
+      if (threadIdx.x == 0) {
+        record_status(P.status, HGB_ERR_TIMEOUT);
+        // both copies may still land: wait once more (bounded) for each
+        mbar_wait(&bar[buf], (k >> 1) & 1);
+        if (s_tile[buf ^ 1] < P.ntiles) mbar_wait(&bar[buf ^ 1], ((k + 1) >> 1) & 1);
+      }
+      break;  // this CTA's remaining tiles are missing; the status word reports the launch as failed
+    }
+    const int tx_ = t % P.tiles_x, r_ = t / P.tiles_x;
+    const int i0 = tx_ * T_TW, j0 = (r_ % P.tiles_y) * T_TH, b = r_ / P.tiles_y;
+    const int X0 = i0 - 16, Y0 = j0 - 1;
+    if (X0 + 15 < 0 || X0 + 145 > p.w || Y0 < 0 || Y0 + T_SH > p.h) {
+      sobel_patch(p, p.in + (int64_t)b * p.in_bstride, tile[buf], X0, Y0);
+      __syncthreads();
+    }
+    const int xo = i0 + 4 * lane, jw = j0 + warp * T_R;
+    if (jw < p.h) {
+      uint32_t tsum = 0;
+      uint8_t *out_row = p.out + (int64_t)b * p.out_bstride + (int64_t)jw * p.out_pitch + xo;
+      const uint8_t *wt = tile[buf] + warp * T_R * T_SW;
+      if (p.vec_out && i0 + T_TW <= p.w && jw + T_R <= p.h)
+        sobel_tile<true, T_R>(p, wt, out_row, xo, jw, 16 + 4 * lane, tsum, tmax);
+      else
+        sobel_tile<false, T_R>(p, wt, out_row, xo, jw, 16 + 4 * lane, tsum, tmax);
+      tsum64 += tsum;
+    }
+    __syncthreads();  // every read of tile[buf] and of s_tile is done
+    if (threadIdx.x == 0) {
+      const int tn = (int)atomicAdd(P.claim, 1u);
+      s_tile[buf] = tn;
+      if (tn < P.ntiles) {
+        fence_proxy_async_smem();
+        issue(buf, tn);
+      }
+    }
+  }
+  const float2 mf = __half22float2(tmax);
+  for (int d = 16; d > 0; d >>= 1) tsum64 += __shfl_xor_sync(0xffffffffu, tsum64, d);
+  const uint32_t bmax = __reduce_max_sync(0xffffffffu, (uint32_t)fmaxf(mf.x, mf.y));
+  if (lane == 0) {
+    s_sum[warp] = tsum64;
+    s_max[warp] = bmax;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long S = 0, M = 0;
+#pragma unroll
+    for (int i = 0; i < T_WARPS; ++i) {
+      S += s_sum[i];
+      M = M > s_max[i] ? M : s_max[i];
+    }
+    if (S) atomicAdd(P.acc, S);
+    if (M) atomicMax(P.acc + 1, M);
+    if (ticket_acq_rel(P.ticket) == gridDim.x - 1) {
+      // every CTA has made its last claim and added its partials
+      const unsigned long long sum = ld_relaxed_u64(P.acc), mx = ld_relaxed_u64(P.acc + 1);
+      if (p.sum_dev) *p.sum_dev = sum;
+      if (p.max_dev) *p.max_dev = (uint32_t)mx;
+      P.acc[0] = 0ull;
+      P.acc[1] = 0ull;
+      *P.claim = 0u;
+      *P.ticket = 0u;
     }
   }
 }
@@ -517,19 +637,31 @@ extern "C" int hgb_sobel_mag(const hgb_view *in, const hgb_view *out, const int 
     rc = make_tensor_map_3d(&P.map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, in->data, p.w, p.h, in->batch, in->pitch,
                             in->batch_stride, T_SW, T_SH);
     if (rc == HGB_OK) {
-      if (sum_dev || max_dev) {
-        Workspace ws;
-        rc = workspace_get(0, &ws);
-        if (rc) return rc;
-        P.acc = ws.acc + kSlotSobel;
-        P.ticket = ws.tickets + 0;
-      }
+      // the streaming form always takes a ticket (it resets its tile counter)
+      Workspace ws;
+      rc = workspace_get(0, &ws);
+      if (rc) return rc;
+      P.acc = ws.acc + kSlotSobel;
+      P.ticket = ws.tickets + 0;
+      P.claim = ws.tickets + kTicketSobelClaim;
       char key[96];
       snprintf(key, sizeof(key), "sobel3:%dx%dx%d", 1 << (32 - __builtin_clz((unsigned)p.w)),
                1 << (32 - __builtin_clz((unsigned)p.h)), in->batch);
       return autotune_run(key, kSobelCfgs, st, [&](int cfg) {
+        const int per_sm = kSobelStream[cfg], warps = kSobelWarps[cfg];
+        if (per_sm > 0) {
+          const void *fn = warps == 8 ? (const void *)sobel3_stream_kernel<8> : (const void *)sobel3_stream_kernel<4>;
+          const int fit = resident_ctas(fn, warps * 32, 0);
+          const int grid = std::max(1, std::min(P.ntiles, num_sms() * std::max(1, std::min(per_sm, fit))));
+          cudaEvent_t ev = before_launch(st);
+          if (warps == 8)
+            sobel3_stream_kernel<8><<<grid, 256, 0, st>>>(P);
+          else
+            sobel3_stream_kernel<4><<<grid, 128, 0, st>>>(P);
+          return after_launch("sobel3_stream_kernel", st, ev);
+        }
         cudaEvent_t ev = before_launch(st);
-        if (kSobelWarps[cfg] == 8)
+        if (warps == 8)
           sobel3_tma_kernel<8><<<P.ntiles, 256, 0, st>>>(P);
         else
           sobel3_tma_kernel<4><<<P.ntiles, 128, 0, st>>>(P);

@@ -60,12 +60,14 @@ def test_sobel_pitched_tma_path(gpu, oracle, b, hw):
         assert m.item() == max(int(r.max()) for r in refs)
 
 
-@pytest.mark.parametrize("cfg", [0, 1])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
 def test_sobel_every_tile_configuration(gpu, oracle, cfg, tmp_path):
     """Each configuration the autotuner can choose for the staged Sobel (rows
-    per warp), forced through a loaded choice file, is bit-exact: ragged
-    tiles, warps whose rows lie below the image, every boundary mode,
-    low-contrast images whose maximum is below 255, a batch."""
+    per warp; one CTA per tile, or a few CTAs per SM claiming tiles), forced
+    through a loaded choice file, is bit-exact: ragged tiles, warps whose rows
+    lie below the image, every boundary mode, low-contrast images whose
+    maximum is below 255, a batch, and calls with and without the fused
+    sum / max one after the other (the claim counter returns to zero)."""
     import json
 
     from hipacc_gb300 import _lib as L
@@ -88,10 +90,16 @@ def test_sobel_every_tile_configuration(gpu, oracle, cfg, tmp_path):
         s = torch.zeros(1, dtype=torch.int64, device="cuda")
         m = torch.zeros(1, dtype=torch.int32, device="cuda")
         src, dst = (dev[:, :, :w], out[:, :, :w]) if nb > 1 else (dev[0, :, :w], out[0, :, :w])
+        gpu.sobel_mag(src, dst, boundary=bnd, const=17)  # no sum / max
+        torch.cuda.synchronize()
+        refs = [oracle.sobel_mag(imgs[i], boundary=bnd, const=17) for i in range(nb)]
+        got = out.cpu().numpy()
+        for i, ref in enumerate(refs):
+            assert np.array_equal(got[i, :, :w], ref), (h, w, bnd, i)
+        out.zero_()
         gpu.sobel_mag(src, dst, boundary=bnd, const=17, sum_out=s, max_out=m)
         torch.cuda.synchronize()
         L.call("hgb_autotune_clear")
-        refs = [oracle.sobel_mag(imgs[i], boundary=bnd, const=17) for i in range(nb)]
         got = out.cpu().numpy()
         for i, ref in enumerate(refs):
             assert np.array_equal(got[i, :, :w], ref), (h, w, bnd, i)
