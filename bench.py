@@ -45,7 +45,7 @@ NSETS = 16
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel on
 # this workload (profiles/ holds the summary and the command); most of each
 # kernel's output is still in L2 when the capture ends, so writes read low
-NCU_TRAFFIC = {"sobel3_tma_kernel": 16845056 + 0, "gray_bulk_kernel": 67121664 + 1593088}
+NCU_TRAFFIC = {"sobel3_tma_kernel": 16845312 + 0, "gray_bulk_kernel": 67121152 + 1238016}
 E2E_STEPS = 64  # end-to-end steps timed, independent of --steps
 METRIC = "Gpixels/s (Sobel3x3 MIRROR + u64 sum + u8 max, and RGBA->gray, 4096x4096)"
 

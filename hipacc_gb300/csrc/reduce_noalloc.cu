@@ -23,7 +23,7 @@
 // Set-up: host code cannot use the array's name as a device address (it is a
 // host-side stand-in).  The first call on a device, with that device current,
 // resolves the address once with cudaGetSymbolAddress and caches it per
-// device; make that first call before any stream capture.
+// device.
 #include <mutex>
 
 #include "reduce_kernels.cuh"

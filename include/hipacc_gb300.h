@@ -296,8 +296,8 @@ HGB_API int hgb_reduce(const hgb_view *in, const hgb_window *win, int op, void *
  * scratch is a fixed 16.25 KiB array in the library's device memory (block
  * partials for at most 1024 blocks; larger launches return HGB_ERR_LIMIT),
  * held by every GPU that loads the library until exit.  The first call on a
- * device resolves the array's address (make it before any stream capture).
- * Every call shares the array: calls that overlap on the GPU race.  Same
+ * device resolves the array's address.  Every call shares the array: calls
+ * that overlap on the GPU race.  Same
  * arguments, results and determinism as hgb_reduce. */
 HGB_API int hgb_reduce_noalloc(const hgb_view *in, const hgb_window *win, int op, void *result_dev,
                                void *result_host, void *stream);
