@@ -197,24 +197,6 @@ __global__ void __launch_bounds__(256) convert_kernel(const char *in, int64_t ip
 // one fma as nvcc and aarch64 GCC do) and runtime/hipacc_cu_interpolate.hpp:173-216.
 __device__ __forceinline__ float mapped(float s, int x) { return __fmaf_rn(s, (float)x, s * 0.5f); }
 
-__device__ __forceinline__ float lf_sample(const float *src, int64_t sp, int sw, int sh, float xm, float ym) {
-  float xb = xm - 0.5f, yb = ym - 0.5f;
-  xb = xb < 0.0f ? 0.0f : xb;
-  yb = yb < 0.0f ? 0.0f : yb;
-  const int xi = (int)xb, yi = (int)yb;
-  const float xf = xb - (float)xi, yf = yb - (float)yi;
-  const int x0 = min(xi, sw - 1), x1 = min(xi + 1, sw - 1), y0 = min(yi, sh - 1), y1 = min(yi + 1, sh - 1);
-  const float *r0 = reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + y0 * sp);
-  const float *r1 = reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + y1 * sp);
-  const float wa = __fmul_rn(1.0f - xf, 1.0f - yf), wb = __fmul_rn(xf, 1.0f - yf);
-  const float wc = __fmul_rn(1.0f - xf, yf), wd = __fmul_rn(xf, yf);
-  float r = __fmul_rn(wa, __ldg(r0 + x0));
-  r = __fmaf_rn(wb, __ldg(r0 + x1), r);
-  r = __fmaf_rn(wc, __ldg(r1 + x0), r);
-  r = __fmaf_rn(wd, __ldg(r1 + x1), r);
-  return r;
-}
-
 // B5 / CF / L3 accessors of the CPU back end (runtime/hipacc_cpu_interpolate.hpp:
 // binomial5, bicubic_spline with a = -0.5, lanczos with l = 3), every product
 // and sum rounded separately in the macros' order, taps clamped to the image.
@@ -319,32 +301,152 @@ __global__ void __launch_bounds__(256) resample_filtered_kernel(const char *in, 
   reinterpret_cast<float *>(out + (int64_t)b * obs + (int64_t)y * op)[x] = acc_out;
 }
 
+// Filtered modes, separable form.  In the order above, the row sum of tap row
+// k (the rounded products over j, summed from j = 0) depends only on the
+// source row and the output column, so every output row whose taps include
+// that source row uses the same number.  A CTA takes a 64 x 32 output tile:
+// its 256 threads first compute the row sums of the R source rows the tile
+// needs (R <= RF_MAXR, checked by the host from the scale) for the tile's 64
+// columns into shared memory, then every output of the tile from them.  Same
+// operations in the same order as resample_filtered_kernel, so the same bits.
+// L3 also keeps the second row's variant (its fifth tap weighed with the sixth
+// weight) for every source row.
+constexpr int RF_TW = 64, RF_TH = 32, RF_MAXR = 64;
+template <int N, bool L3>
+__global__ void __launch_bounds__(256) resample_sep_kernel(const char *in, int64_t ip, int64_t ibs, int sw, int sh,
+                                                           char *out, int64_t op, int64_t obs, int dw, int dh,
+                                                           const ResTap *cols, const ResTap *rows, int *status) {
+  __shared__ float hs[(L3 ? 2 : 1) * RF_MAXR * RF_TW];
+  __shared__ int s_first[RF_TH];
+  __shared__ float s_w[RF_TH][N];
+  const int c = threadIdx.x & (RF_TW - 1), rg = threadIdx.x / RF_TW;
+  const int x0 = blockIdx.x * RF_TW, y0 = blockIdx.y * RF_TH, b = blockIdx.z;
+  const int x = x0 + c, nrow = min(RF_TH, dh - y0);
+  if ((int)threadIdx.x < nrow) {
+    const ResTap cy = rows[y0 + threadIdx.x];
+    s_first[threadIdx.x] = cy.first;
+#pragma unroll
+    for (int k = 0; k < N; ++k) s_w[threadIdx.x][k] = cy.w[k];
+  }
+  const int r0 = rows[y0].first;
+  const int R = rows[y0 + nrow - 1].first + N - r0;
+  if (R > RF_MAXR) {  // the host keeps the scale in range; never taken
+    if (threadIdx.x == 0) record_status(status, HGB_ERR_INTERNAL);
+    return;
+  }
+  const float *src = reinterpret_cast<const float *>(in + (int64_t)b * ibs);
+  if (x < dw) {
+    const ResTap cx = cols[x];
+    int xs[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) xs[j] = min(max(cx.first + j, 0), sw - 1);
+    for (int r = rg; r < R; r += 256 / RF_TW) {
+      const int yy = min(max(r0 + r, 0), sh - 1);
+      const float *row = reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + yy * ip);
+      float v[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) v[j] = __ldg(row + xs[j]);
+      float acc = __fmul_rn(v[0], cx.w[0]);
+#pragma unroll
+      for (int j = 1; j < N; ++j) acc = __fadd_rn(acc, __fmul_rn(v[j], cx.w[j]));
+      hs[r * RF_TW + c] = acc;
+      if constexpr (L3) {
+        float a2 = __fmul_rn(v[0], cx.w[0]);
+#pragma unroll
+        for (int j = 1; j < N; ++j) a2 = __fadd_rn(a2, __fmul_rn(v[j], cx.w[j == 4 ? 5 : j]));
+        hs[RF_MAXR * RF_TW + r * RF_TW + c] = a2;
+      }
+    }
+  }
+  __syncthreads();
+  if (x >= dw) return;
+  float *dst = reinterpret_cast<float *>(out + (int64_t)b * obs) + x;
+  for (int yl = rg; yl < nrow; yl += 256 / RF_TW) {
+    const int base = s_first[yl] - r0;
+    float acc_out = 0.0f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      const float h = hs[((L3 && k == 1) ? RF_MAXR * RF_TW : 0) + (base + k) * RF_TW + c];
+      const float q = __fmul_rn(h, s_w[yl][k]);
+      acc_out = k == 0 ? q : __fadd_rn(acc_out, q);
+    }
+    *reinterpret_cast<float *>(reinterpret_cast<char *>(dst) + (int64_t)(y0 + yl) * op) = acc_out;
+  }
+}
+
 // NN and LF: a thread per column and four rows 8 apart (a 32 x 32 block of
 // outputs per CTA), so that every thread has four independent reads in flight
 constexpr int RS_ROWS = 4;
+// Sample positions along one axis, evaluated once per CTA for its 32 columns
+// and 32 rows instead of once per pixel.  NN keeps the clamped index of the
+// mapped coordinate.  LF keeps, for b = max(mapped - 0.5, 0), the clamped
+// indices of floor(b) and floor(b) + 1 and the weights (1 - f, f) of the
+// fraction f; the pixel's four weights are the rounded products of a column
+// weight and a row weight, and the sum is w00 v00 rounded, then three fused
+// multiply-adds in the order (x1, y0), (x0, y1), (x1, y1).
+struct RsAxis {
+  int i0, i1;
+  float w0, w1;
+};
+__device__ __forceinline__ RsAxis rs_axis(float s, int o, int n, bool lf) {
+  const float m = mapped(s, o);
+  RsAxis a;
+  if (!lf) {
+    a.i0 = a.i1 = min(max((int)m, 0), n - 1);
+    a.w0 = a.w1 = 0.0f;
+    return a;
+  }
+  float bpos = m - 0.5f;
+  bpos = bpos < 0.0f ? 0.0f : bpos;
+  const int bi = (int)bpos;
+  const float f = bpos - (float)bi;
+  a.i0 = min(bi, n - 1);
+  a.i1 = min(bi + 1, n - 1);
+  a.w0 = 1.0f - f;
+  a.w1 = f;
+  return a;
+}
+
 __global__ void __launch_bounds__(256) resample_kernel(const char *in, int64_t ip, int64_t ibs, int sw, int sh,
                                                        char *out, int64_t op, int64_t obs, int dw, int dh, int imode) {
-  const int x = blockIdx.x * 32 + threadIdx.x, b = blockIdx.z;
+  __shared__ RsAxis s_col[32], s_row[8 * RS_ROWS];
+  const int x = blockIdx.x * 32 + threadIdx.x, b = blockIdx.z, yb = blockIdx.y * 8 * RS_ROWS;
+  const bool lf = imode != 1;
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  if (t < 32) {
+    const int xc = blockIdx.x * 32 + t;
+    if (xc < dw) s_col[t] = rs_axis((float)sw / (float)dw, xc, sw, lf);
+  } else if (t < 32 + 8 * RS_ROWS) {
+    const int yr = yb + t - 32;
+    if (yr < dh) s_row[t - 32] = rs_axis((float)sh / (float)dh, yr, sh, lf);
+  }
+  __syncthreads();
   if (x >= dw) return;
-  const float sx = (float)sw / (float)dw, sy = (float)sh / (float)dh;
-  const float *src = reinterpret_cast<const float *>(in + (int64_t)b * ibs);
+  const RsAxis cx = s_col[threadIdx.x];
+  const char *src = in + (int64_t)b * ibs;
   float v[RS_ROWS];
 #pragma unroll
   for (int k = 0; k < RS_ROWS; ++k) {
-    const int y = blockIdx.y * 8 * RS_ROWS + threadIdx.y + 8 * k;
-    if (y >= dh) break;
-    if (imode == 1) {
-      int xx = (int)mapped(sx, x), yy = (int)mapped(sy, y);
-      xx = min(max(xx, 0), sw - 1);
-      yy = min(max(yy, 0), sh - 1);
-      v[k] = __ldg(reinterpret_cast<const float *>(reinterpret_cast<const char *>(src) + yy * ip) + xx);
+    const int yl = threadIdx.y + 8 * k;
+    if (yb + yl >= dh) break;
+    const RsAxis ry = s_row[yl];
+    const float *r0 = reinterpret_cast<const float *>(src + ry.i0 * ip);
+    if (!lf) {
+      v[k] = __ldg(r0 + cx.i0);
     } else {
-      v[k] = lf_sample(src, ip, sw, sh, mapped(sx, x), mapped(sy, y));
+      const float *r1 = reinterpret_cast<const float *>(src + ry.i1 * ip);
+      const float wa = __fmul_rn(cx.w0, ry.w0), wb = __fmul_rn(cx.w1, ry.w0);
+      const float wc = __fmul_rn(cx.w0, ry.w1), wd = __fmul_rn(cx.w1, ry.w1);
+      float r = __fmul_rn(wa, __ldg(r0 + cx.i0));
+      r = __fmaf_rn(wb, __ldg(r0 + cx.i1), r);
+      r = __fmaf_rn(wc, __ldg(r1 + cx.i0), r);
+      r = __fmaf_rn(wd, __ldg(r1 + cx.i1), r);
+      v[k] = r;
     }
   }
 #pragma unroll
   for (int k = 0; k < RS_ROWS; ++k) {
-    const int y = blockIdx.y * 8 * RS_ROWS + threadIdx.y + 8 * k;
+    const int y = yb + threadIdx.y + 8 * k;
     if (y >= dh) break;
     reinterpret_cast<float *>(out + (int64_t)b * obs + (int64_t)y * op)[x] = v[k];
   }
@@ -567,6 +669,22 @@ extern "C" int hgb_resample(const hgb_view *in, const hgb_view *out, int imode, 
                                                                              out->width, out->height, imode);
   const char *src = (const char *)in->data;
   char *dst = (char *)out->data;
+  // the separable form holds the row sums of at most RF_MAXR source rows per
+  // 32 output rows: first taps advance by at most ceil(31 * sh / dh) + 1 rows
+  const int n = imode == 5 ? 6 : 4;
+  if ((double)in->height / out->height * (RF_TH - 1) + 2 + n <= RF_MAXR) {
+    const dim3 gs(cdiv(out->width, RF_TW), cdiv(out->height, RF_TH), out->batch);
+    int *status = device_status_word();
+    if (imode == 5)
+      resample_sep_kernel<6, true><<<gs, 256, 0, st>>>(src, in->pitch, in->batch_stride, in->width, in->height, dst,
+                                                       out->pitch, out->batch_stride, out->width, out->height, cols,
+                                                       rows, status);
+    else
+      resample_sep_kernel<4, false><<<gs, 256, 0, st>>>(src, in->pitch, in->batch_stride, in->width, in->height,
+                                                        dst, out->pitch, out->batch_stride, out->width, out->height,
+                                                        cols, rows, status);
+    return after_launch("resample_sep_kernel", st, ev);
+  }
   if (imode == 5)
     resample_filtered_kernel<6, true><<<grid, block, 0, st>>>(src, in->pitch, in->batch_stride, in->width,
                                                               in->height, dst, out->pitch, out->batch_stride,

@@ -15,8 +15,13 @@ pytestmark = pytest.mark.gpu
 L3_TOL = 2e-6
 
 
+# Scales up to about 1.9 source rows per output row take the separable tiled
+# kernel (row sums in shared memory); larger ones the direct kernel.  Shapes
+# cover both, several tiles, ragged tile edges and the benchmark's 2x scale.
 @pytest.mark.parametrize("shape", [((17, 23), (40, 31)), ((64, 48), (16, 20)), ((300, 500), (611, 997)),
-                                   ((9, 9), (9, 9)), ((5, 7), (3, 2))])
+                                   ((9, 9), (9, 9)), ((5, 7), (3, 2)), ((100, 80), (60, 50)),
+                                   ((1000, 700), (513, 400)), ((256, 200), (1024, 777)),
+                                   ((1024, 1024), (2048, 2048)), ((33, 2000), (70, 130))])
 @pytest.mark.parametrize("mode", ["b5", "cf", "l3"])
 def test_filtered_resampling(gpu, oracle, shape, mode):
     (sh, sw), (dh, dw) = shape
@@ -41,3 +46,31 @@ def test_filtered_resampling_batch(gpu, oracle):
     torch.cuda.synchronize()
     for b in range(3):
         assert np.array_equal(out[b].cpu().numpy(), oracle.resample_filtered(src[b], 90, 25, "cf", contract=1))
+
+
+@pytest.mark.parametrize("shape", [((17, 23), (40, 31)), ((64, 48), (16, 20)), ((300, 500), (611, 997)),
+                                   ((9, 9), (9, 9)), ((5, 7), (3, 2)), ((1, 1), (7, 5)), ((1000, 700), (513, 400)),
+                                   ((1024, 1024), (2048, 2048)), ((33, 2000), (70, 130))])
+@pytest.mark.parametrize("mode", ["nn", "lf"])
+def test_nn_lf_resampling(gpu, oracle, shape, mode):
+    """Nearest-neighbour and bilinear accessors read as a point operator:
+    bit-exact against the oracle (mapped coordinate as one fused multiply-add,
+    the bilinear sum as a rounded product and three fused multiply-adds)."""
+    (sh, sw), (dh, dw) = shape
+    rng = np.random.default_rng(sh * 7 + dw)
+    src = rng.random((sh, sw), dtype=np.float32)
+    out = torch.empty((dh, dw), dtype=torch.float32, device="cuda")
+    gpu.resample(torch.from_numpy(src).cuda(), out, mode=mode)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), oracle.resample(src, dw, dh, mode, contract=1))
+
+
+def test_nn_lf_resampling_batch(gpu, oracle):
+    rng = np.random.default_rng(78)
+    src = rng.random((3, 40, 60), dtype=np.float32)
+    for mode in ("nn", "lf"):
+        out = torch.empty((3, 77, 50), dtype=torch.float32, device="cuda")
+        gpu.resample(torch.from_numpy(src).cuda(), out, mode=mode)
+        torch.cuda.synchronize()
+        for b in range(3):
+            assert np.array_equal(out[b].cpu().numpy(), oracle.resample(src[b], 50, 77, mode, contract=1)), mode
