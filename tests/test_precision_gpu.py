@@ -74,6 +74,36 @@ def test_separable_many_tiles(gpu, oracle, dtype, b):
     assert torch.equal(got, ref)
 
 
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("k", [3, 5, 7, 9, 11, 13, 15])
+def test_separable_tma_half_storage(gpu, oracle, dtype, k):
+    """16-bit storage with rows padded to 16 bytes takes the TMA-staged form:
+    bit-exact for every mask size, every boundary, ragged and odd widths,
+    images shorter than the mask, several tiles in both directions, and a
+    batch."""
+    rng = np.random.default_rng(100 + k)
+    taps = oracle.gaussian_taps(k, 2.0)
+    cases = [((517, 1301), 1, 1), ((300, 130), 2, 1), ((1, 9), 3, 1), ((5, 3), 4, 1), ((257, 129), 3, 2),
+             ((600, 256), 4, 1), ((33, 700), 2, 3)]
+    for (h, w), b, nb in cases:
+        img = field(h, w * nb, k + b)[:, :w * nb].reshape(h, nb, w).transpose(1, 0, 2).copy()
+        img = np.clip(img + rng.normal(0, 0.01, img.shape).astype(np.float32), 0, 1)
+        src = torch.from_numpy(img).to(dtype)
+        wp = (w + 7) // 8 * 8 + 8
+        dev = torch.zeros((nb, h, wp), dtype=dtype, device="cuda")
+        dev[:, :, :w] = src.cuda()
+        out = torch.full((nb, h, wp), 3.0, dtype=dtype, device="cuda")
+        s_in, s_out = (dev[:, :, :w], out[:, :, :w]) if nb > 1 else (dev[0, :, :w], out[0, :, :w])
+        gpu.separable(s_in, s_out, taps, taps, boundary=b, const=0.5)
+        torch.cuda.synchronize()
+        got = out.cpu()
+        for i in range(nb):
+            ref = torch.from_numpy(oracle.separable(src[i].float().numpy(), taps, taps, boundary=b, const=0.5,
+                                                    contract=1)).to(dtype)
+            assert torch.equal(got[i, :, :w], ref), (k, h, w, b, i)
+            assert torch.all(got[i, :, w:] == 3.0)  # nothing written past the width
+
+
 @pytest.mark.parametrize("b", [2, 4])
 def test_separable_8192(gpu, oracle, b):
     """The 9x9 sigma=2 separable Gaussian on the 8192x8192 field, REPEAT and CONSTANT(0.5)."""
