@@ -358,7 +358,9 @@ def run_gb300(args):
                        "images_per_step": "1 u8 + 1 uchar4", "pixels_per_step": PX_PER_STEP,
                        "resident_sets": NSETS, "l2": f"inputs larger than L2 ({NSETS} rotating sets, "
                                                      f"{NSETS * 117} MB)", "launch": "CUDA graph replay: graphs of up to 64 steps, each a Sobel chain and a gray chain on two streams",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       "warmup_detail": f"{max(3, args.warmup)} steps, then one untimed replay of each timed graph "
+                                        f"({args.steps} steps) so that no timed launch is a graph's first"},
             "roofline": {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
                          "frac": dom["achieved_gbs"] / peak, "traffic": NCU_TRAFFIC.get(dom_name), "kernel": dom_name,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},
