@@ -227,7 +227,8 @@ def test_sobel_tma_pitched(gpu, oracle, hw, b):
 
 
 def test_sobel_batch_tma(gpu, oracle):
-    """A batch through one persistent launch; sum / max cover the whole batch."""
+    """A batch of three images in one launch (one CTA per tile of every image);
+    the fused sum / max cover the whole batch."""
     rng = np.random.default_rng(12)
     imgs = rng.integers(0, 256, (3, 200, 256), dtype=np.uint8)
     t = torch.from_numpy(imgs).cuda()

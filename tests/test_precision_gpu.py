@@ -63,8 +63,9 @@ def test_separable_half_storage(gpu, oracle, dtype, b):
 @pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16, torch.float16])
 @pytest.mark.parametrize("b", [1, 2, 3, 4])
 def test_separable_many_tiles(gpu, oracle, dtype, b):
-    """A multi-tile image with ragged edges: the persistent TMA form walks many
-    tiles per CTA through two buffers; bit-exact in every storage type."""
+    """A multi-tile image with ragged edges and unpadded rows of 1301 elements,
+    which no storage type aligns to 16 bytes, so the tiles are staged with
+    plain loads instead of TMA: bit-exact in every storage type."""
     img = field(517, 1301, 7 + b)
     src = torch.from_numpy(img).to(dtype)
     taps = oracle.gaussian_taps(9, 2.0)
