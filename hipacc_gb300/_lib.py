@@ -94,6 +94,8 @@ SIGNATURES = {
     "hgb_pyramid_plan_trace": (i32, [vp, vp, C.c_longlong]),
     "hgb_local_op_adjoint": (i32, [VP, VP, VP, vp, vp, i32, i32, i32, vp, vp]),
     "hgb_bilateral_adjoint": (i32, [VP, VP, vp, i32, f32, i32, f32, VP, vp, vp]),
+    "hgb_separable_adjoint": (i32, [VP, VP, vp, vp, i32, i32, f32, VP, vp, vp, vp]),
+    "hgb_local_op_minmax_adjoint": (i32, [VP, VP, VP, vp, vp, i32, i32, i32, i32, f32, vp]),
     "hgb_conv_bilateral_mse": (i32, [VP, VP, vp, i32, vp, i32, vp, i32, i32, vp, VP, vp, vp, vp]),
 }
 

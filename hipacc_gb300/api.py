@@ -334,6 +334,47 @@ def bilateral_adjoint(inp, grad_out, smask, sigma_r, boundary=CLAMP, const=0.0, 
     return gi, gs
 
 
+def separable_adjoint(inp, grad_out, row_taps, col_taps=None, boundary=CLAMP, const=0.0, want_grad_in=True,
+                      want_grad_taps=True, stream=None):
+    """Adjoint of the separable filter (FP32): (grad_in, grad_row, grad_col)."""
+    r = np.ascontiguousarray(row_taps, np.float32)
+    c = np.ascontiguousarray(col_taps if col_taps is not None else row_taps, np.float32)
+    gi = torch.empty_like(grad_out) if want_grad_in else None
+    gr = torch.zeros(len(r), dtype=torch.float32, device=grad_out.device) if want_grad_taps else None
+    gc = torch.zeros(len(r), dtype=torch.float32, device=grad_out.device) if want_grad_taps else None
+    vi, vg = view(inp), view(grad_out)
+    vgi = view(gi) if gi is not None else None
+    L.call("hgb_separable_adjoint", C.byref(vi), C.byref(vg), r.ctypes.data_as(C.c_void_p),
+           c.ctypes.data_as(C.c_void_p), len(r), boundary, float(const), None if vgi is None else C.byref(vgi),
+           None if gr is None else C.c_void_p(gr.data_ptr()), None if gc is None else C.c_void_p(gc.data_ptr()),
+           _stream(stream))
+    return gi, gr, gc
+
+
+def minmax_adjoint(inp, grad_out, reduce, mask=None, domain=None, size=None, boundary=CLAMP, const=0.0, stream=None):
+    """Adjoint of the MIN / MAX local operator (Domain reduce or convolve with a
+    mask): grad_in for grad_out = dL/dout."""
+    if mask is not None:
+        m = np.ascontiguousarray(mask, np.float32)
+        mh, mw = m.shape
+        mp = m.ctypes.data_as(C.c_void_p)
+    else:
+        m, mp = None, None
+    if domain is not None:
+        d = np.ascontiguousarray(domain, np.uint8)
+        mh, mw = d.shape
+        dp = d.ctypes.data_as(C.c_void_p)
+    else:
+        d, dp = None, None
+    if m is None and d is None:
+        mh = mw = int(size)
+    gi = torch.empty_like(grad_out)
+    vi, vg, vgi = view(inp), view(grad_out), view(gi)
+    L.call("hgb_local_op_minmax_adjoint", C.byref(vi), C.byref(vg), C.byref(vgi), mp, dp, mw, mh, reduce, boundary,
+           float(const), _stream(stream))
+    return gi
+
+
 def harris(inp, out=None, k=0.04, threshold=20000.0, boundary=CLAMP, mode=0, stream=None):
     """The Harris corner program (u8 in, 0 / 1 u8 out); mode 0 fused, 1 nine launches."""
     if out is None:

@@ -369,7 +369,9 @@ HGB_API int hgb_pyramid_plan_trace(hgb_pyramid_plan *plan, long long *trace_dev,
  * through the remap, CONSTANT taps carry no gradient.
  *   grad_in  (may be NULL) = conv^T(grad_out)
  *   grad_mask_dev (may be NULL, mask_w*mask_h floats) = sum_p grad_out(p) * in(remap(p+c)),
- *   deterministic: block partials combined in FP64 in a fixed order.
+ *   deterministic: block partials combined in FP64 in a fixed order.  With
+ *   CONSTANT, taps outside the image count as reading 0 in grad_mask (the
+ *   constant is not an argument here): exact for a forward with constant 0. 
  * mask is a device array (mask_dev) or host array (mask). */
 HGB_API int hgb_local_op_adjoint(const hgb_view *in, const hgb_view *grad_out, const hgb_view *grad_in, const float *mask,
                          const float *mask_dev, int mask_w, int mask_h, int boundary, float *grad_mask_dev,
@@ -391,6 +393,39 @@ HGB_API int hgb_local_op_adjoint(const hgb_view *in, const hgb_view *grad_out, c
 HGB_API int hgb_bilateral_adjoint(const hgb_view *in, const hgb_view *grad_out, const float *smask, int size,
                                   float sigma_r, int boundary, float const_val, const hgb_view *grad_in,
                                   float *grad_sigma_dev, void *stream);
+
+/* Adjoint of the separable filter hgb_separable (FP32 storage).  The forward
+ * is the reference's two local operators, t = conv(in, row taps as 1 x K)
+ * and out = conv(t, column taps as K x 1), each with the boundary (the
+ * separable form has no reference primitive: lib/AST/Convolution.cpp:397-435
+ * is the 2-D convolve it splits).  For grad_out = dL/dout:
+ *   grad_in (may be NULL)               = dL/din, boundary transposed as in
+ *                                         hgb_local_op_adjoint;
+ *   grad_row_dev, grad_col_dev (may be
+ *   NULL, k floats each, device)        = dL/drow_taps, dL/dcol_taps, combined in
+ *                                         FP64 in a fixed order.
+ * Same taps / k / boundary / const_val as the forward (const_val recomputes t;
+ * the tap gradients count CONSTANT taps outside as reading 0).  Composed from
+ * hgb_local_op and hgb_local_op_adjoint; uses the library workspace (8 bytes
+ * per pixel): calls sharing it must be ordered on one stream. */
+HGB_API int hgb_separable_adjoint(const hgb_view *in, const hgb_view *grad_out, const float *row_taps,
+                                  const float *col_taps, int k, int boundary, float const_val,
+                                  const hgb_view *grad_in, float *grad_row_dev, float *grad_col_dev, void *stream);
+
+/* Adjoint of the MIN / MAX local operator: Kernel::reduce(Domain,
+ * Reduce::MIN/MAX) (domain given, mask NULL) and Kernel::convolve(mask,
+ * Reduce::MIN/MAX) (mask given, domain NULL or all ones); dsl/kernel.hpp:241-315,
+ * lib/AST/Convolution.cpp:43-100.  The forward starts at FLT_MAX (MIN) or
+ * FLT_MIN (MAX) and takes acc = acc < v ? acc : v (MIN) or acc > v ? acc : v
+ * (MAX) per tap in row-major order.  Each output's gradient goes to the pixel
+ * read by the tap that last replaced the running value (times its mask weight
+ * for convolve); nothing flows when no tap replaced the initial value or when
+ * the winner was a CONSTANT tap outside the image.  grad_in is gathered per
+ * pixel in a fixed order (deterministic).  FP32 storage, masks up to 15 x 15.
+ * Uses the library workspace (1 byte per pixel). */
+HGB_API int hgb_local_op_minmax_adjoint(const hgb_view *in, const hgb_view *grad_out, const hgb_view *grad_in,
+                                        const float *mask, const uint8_t *domain, int mask_w, int mask_h,
+                                        int reduce, int boundary, float const_val, void *stream);
 
 /* Forward + adjoint of the differentiation workload
  *   y1 = conv(x, mask), y = bilateral(y1; smask, sigma_r), loss = mean((y - t)^2)
