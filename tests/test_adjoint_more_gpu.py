@@ -186,3 +186,26 @@ def test_minmax_adjoint_batch(gpu, oracle):
     for b in range(2):
         _, ref = minmax64(oracle, img[b], gout[b], True, 3, 0.0, domain=CROSS)
         assert rel(gi[b].cpu().numpy(), ref) <= 2e-6
+
+
+def test_autograd_wrappers(gpu, oracle):
+    """Separable and LocalMinMax as torch.autograd.Functions: backward gives the
+    adjoint entry points' gradients, which match the FP64 restatements."""
+    from hipacc_gb300.autograd import LocalMinMax, Separable
+
+    rng = np.random.default_rng(21)
+    img = rng.random((40, 64)).astype(np.float32)
+    wgt = rng.normal(0, 1, (40, 64)).astype(np.float32)
+    x = torch.from_numpy(img).cuda().requires_grad_(True)
+    w = torch.from_numpy(wgt).cuda()
+    row = torch.from_numpy(rng.normal(0, 1, 5).astype(np.float32)).cuda().requires_grad_(True)
+    col = torch.from_numpy(rng.normal(0, 1, 5).astype(np.float32)).cuda().requires_grad_(True)
+    (Separable.apply(x, row, col, gpu.MIRROR) * w).sum().backward()
+    ref_in, ref_row, ref_col = sep_adjoint64(oracle, img, wgt, row.detach().cpu().numpy(),
+                                             col.detach().cpu().numpy(), 3, 0.0)
+    assert rel(x.grad.cpu().numpy(), ref_in) <= 2e-6
+    assert rel(row.grad.cpu().numpy(), ref_row) <= 1e-5 and rel(col.grad.cpu().numpy(), ref_col) <= 1e-5
+    x.grad = None
+    (LocalMinMax.apply(x, gpu.MAX, CROSS, None, gpu.REPEAT) * w).sum().backward()
+    _, ref = minmax64(oracle, img, wgt, True, 2, 0.0, domain=CROSS)
+    assert rel(x.grad.cpu().numpy(), ref) <= 2e-6
