@@ -400,6 +400,96 @@ def bilateral_adjoint(img, grad_out, smask, sigma_r, boundary=CLAMP, const=0.0):
     return gi, float(ds)
 
 
+def remap_vec(mode, idx, n):
+    """remap() over an index vector; negative where CONSTANT reads the constant."""
+    return np.array([remap(mode, int(i), 0, n) for i in idx], np.int64)
+
+
+def local_op_adjoint(img, grad_out, mask, boundary=CLAMP):
+    """FP64 adjoint of the SUM local operator out(j) = sum_o m_o in(r(j + o))
+    (lib/AST/Convolution.cpp:43-100 with the remap of
+    lib/AST/BorderHandling.cpp:41-120), by scattering: every tap o of every
+    output j sends m_o grad_out(j) to r(j + o); CONSTANT taps send nothing and
+    read 0 in the mask gradient.  Returns (grad_in, grad_mask)."""
+    gout = np.asarray(grad_out, np.float64)
+    img = np.asarray(img, np.float64)
+    mask = np.asarray(mask)
+    h, w = gout.shape
+    mh, mw = mask.shape
+    gin = np.zeros((h, w))
+    gm = np.zeros((mh, mw))
+    ys, xs = np.arange(h), np.arange(w)
+    for my in range(mh):
+        ry = remap_vec(boundary, ys + my - mh // 2, h)
+        for mx in range(mw):
+            rx = remap_vec(boundary, xs + mx - mw // 2, w)
+            Y, X = np.meshgrid(np.where(ry >= 0)[0], np.where(rx >= 0)[0], indexing="ij")
+            np.add.at(gin, (ry[Y], rx[X]), float(mask[my, mx]) * gout[Y, X])
+            gm[my, mx] = np.sum(gout[Y, X] * img[ry[Y], rx[X]])
+    return gin, gm
+
+
+def separable_adjoint(img, grad_out, row_taps, col_taps, boundary=CLAMP, const=0.0):
+    """FP64 adjoint of the separable filter t = rows(in), out = cols(t), each a
+    1-D SUM local operator with the boundary (rows of t outside the image are
+    t's own remap, or the constant).  Returns (grad_in, grad_row, grad_col);
+    the tap gradients count CONSTANT taps outside as reading 0."""
+    x = np.asarray(img, np.float64)
+    h, w = x.shape
+    k = len(row_taps)
+    t = np.zeros((h, w))
+    xs = np.arange(w)
+    for j in range(k):
+        rx = remap_vec(boundary, xs + j - k // 2, w)
+        t += float(row_taps[j]) * np.where((rx >= 0)[None, :], x[:, np.clip(rx, 0, w - 1)], const)
+    gt, gcol = local_op_adjoint(t, grad_out, np.asarray(col_taps).reshape(-1, 1), boundary)
+    gin, grow = local_op_adjoint(x, gt, np.asarray(row_taps).reshape(1, -1), boundary)
+    return gin, grow.ravel(), gcol.ravel()
+
+
+def minmax_adjoint(img, grad_out, reduce, mask=None, domain=None, boundary=CLAMP, const=0.0):
+    """The MIN / MAX local operator and its adjoint.  Forward as the reference
+    evaluates it (lib/AST/Convolution.cpp:43-100, dsl/math_functions.hpp:347-376):
+    acc starts at FLT_MAX (MIN) or FLT_MIN (MAX), and every tap of the Domain
+    (or of the mask, v = m * x in float32 for convolve) in row-major order takes
+    acc = acc < v ? acc : v or acc > v ? acc : v.  The gradient of an output
+    goes to the pixel read by the tap that last replaced the running value
+    (times its mask weight); nothing when no tap replaced the start value or
+    when the winner read the CONSTANT value outside.  Returns (out as float32,
+    grad_in in FP64)."""
+    img = np.asarray(img, np.float32)
+    h, w = img.shape
+    shape = np.asarray(mask if mask is not None else domain).shape
+    mh, mw = shape
+    is_max = reduce == MAX
+    acc = np.full((h, w), np.finfo(np.float32).tiny if is_max else np.finfo(np.float32).max, np.float32)
+    win = np.full((h, w), -1, np.int64)
+    sy = np.zeros((h, w), np.int64)
+    sx = np.zeros((h, w), np.int64)
+    ys, xs = np.arange(h), np.arange(w)
+    for my in range(mh):
+        ry = remap_vec(boundary, ys + my - mh // 2, h)
+        for mx in range(mw):
+            if domain is not None and not domain[my][mx]:
+                continue
+            rx = remap_vec(boundary, xs + mx - mw // 2, w)
+            outside = (ry[:, None] < 0) | (rx[None, :] < 0)
+            RY = np.broadcast_to(np.clip(ry, 0, h - 1)[:, None], (h, w))
+            RX = np.broadcast_to(np.clip(rx, 0, w - 1)[None, :], (h, w))
+            xv = np.where(outside, np.float32(const), img[RY, RX]).astype(np.float32)
+            v = (np.float32(mask[my][mx]) * xv).astype(np.float32) if mask is not None else xv
+            upd = ~(acc > v) if is_max else ~(acc < v)
+            acc = np.where(upd, v, acc)
+            win = np.where(upd, np.where(outside, -1, my * mw + mx), win)
+            sy = np.where(upd, RY, sy)
+            sx = np.where(upd, RX, sx)
+    gin = np.zeros((h, w))
+    ok = win >= 0
+    fac = np.ones(win.shape) if mask is None else np.asarray(mask, np.float64).ravel()[np.maximum(win, 0)]
+    np.add.at(gin, (sy[ok], sx[ok]), (fac * np.asarray(grad_out, np.float64))[ok])
+    return acc, gin
+
+
 # ---- standard masks (FP64 construction rounded once to FP32) ----
 
 def gaussian_mask(size, sigma, dtype=np.float32):
